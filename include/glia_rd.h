@@ -1,0 +1,196 @@
+/*
+ * glia_rd.h — C-ABI of the GB300-native reaction–diffusion forward / adjoint path.
+ *
+ * Model: dc/dt = div(k(x) grad c) + rho(x) c (1 - c) on the periodic grid [0, 2*pi)^3 with n^3
+ * voxels (row-major, z fastest: idx = x*n*n + y*n + z). Strang splitting (order 2) or Lie
+ * splitting (order 1); each diffusion sub-step is Crank–Nicolson solved by PCG with the spectral
+ * mean-diffusivity preconditioner; the logistic reaction sub-step is analytic.
+ *
+ * Every entry point replaces one method of the reference's C++/PETSc classes; the replaced
+ * interface is cited next to each declaration (paths are relative to the GLIA source tree).
+ *
+ * Conventions
+ *  - Every function returns an int status: GLIA_OK (0) or a negative GLIA_ERR_* code.
+ *    glia_last_error(ctx) returns the message of the last failure on that context.
+ *    No C++ exception crosses this boundary.
+ *  - A context owns its device work buffers, cuFFT plans, time history and checkpoints.
+ *    The caller owns every buffer it passes. A context is not thread-safe: use one per host
+ *    thread (and per CUDA stream).
+ *  - Grid fields (n^3 values) are passed as `const void*` / `void*`; their location and element
+ *    type follow the context's pointer mode (glia_set_pointer_mode): host double (default),
+ *    device double or device float. Parameter vectors (p, x, dJ, centers) are always host double.
+ *  - Floating-point state is FP64 (GLIA_FP64) or FP32 bulk with FP64 reductions and FP64
+ *    scalars (GLIA_MIXED). GLIA_ENGINE_REFERENCE restates the reference's GPU structure
+ *    (real-space PCG, one kernel per vector operation, 10 transforms per diffusion apply) and
+ *    exists as the plain baseline; GLIA_ENGINE_FUSED is the fused spectral-space path.
+ */
+#ifndef GLIA_RD_H_
+#define GLIA_RD_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------ */
+#define GLIA_OK 0
+#define GLIA_ERR_INVALID (-1)       /* bad argument or unsupported size                        */
+#define GLIA_ERR_CUDA (-2)          /* CUDA runtime error (message has the CUDA error string)  */
+#define GLIA_ERR_CUFFT (-3)         /* cuFFT plan or execution error                           */
+#define GLIA_ERR_NOT_CONVERGED (-4) /* PCG reached maxit, diverged or hit a NaN                */
+#define GLIA_ERR_STATE (-5)         /* call order: e.g. adjoint before a state solve           */
+#define GLIA_ERR_OOM (-6)           /* device allocation failed                                */
+#define GLIA_ERR_NONFINITE (-7)     /* a non-finite value reached a reduction                  */
+#define GLIA_ERR_NO_DEVICE (-8)     /* no CUDA device is visible                               */
+
+/* ---- context configuration --------------------------------------------------------------- */
+#define GLIA_FP64 0  /* all fields, transforms and reductions in double                        */
+#define GLIA_MIXED 1 /* fields and transforms in float; reductions, PCG scalars, gradients FP64 */
+
+#define GLIA_ENGINE_FUSED 0     /* fused spectral-space PCG (the product path)                  */
+#define GLIA_ENGINE_REFERENCE 1 /* reference-structured plain path (baseline, FP64 or float)    */
+
+#define GLIA_PTR_HOST_F64 0   /* grid fields are host double arrays                            */
+#define GLIA_PTR_DEVICE_F64 1 /* grid fields are device double arrays                          */
+#define GLIA_PTR_DEVICE_F32 2 /* grid fields are device float arrays                           */
+
+/* Time history kept for the adjoint (PdeOperatorsRD ctor, src/pde/PdeOperators.cpp:17-55). */
+#define GLIA_HISTORY_FULL 0       /* every state c_[0..nt] (and c_half_ when adjoint_store) */
+#define GLIA_HISTORY_CHECKPOINT 1 /* every k-th state; segments recomputed in the adjoint    */
+
+/* Which dt the spectral preconditioner is built with (DiffusionSolver::precFactor,
+ * src/pde/DiffusionSolver.cpp:119-180, reads ctx_->dt_, which solve() overwrites at :226). */
+#define GLIA_PC_DT_REFERENCE 0 /* reference rule: dt of the last solve, full dt before any   */
+#define GLIA_PC_DT_FIXED 1     /* the value given to glia_set_pcg                            */
+#define GLIA_PC_DT_MATCHED 2   /* twice the dt of each solve (exact for constant k)          */
+
+typedef struct glia_ctx glia_ctx;
+
+/* Optimizer-side settings read by the derivative operators (include/Parameters.h:17-109). */
+typedef struct glia_opt_settings {
+  int np;                    /* number of Gaussian coefficients p                               */
+  int nk;                    /* number of diffusivity parameters (1..3)                         */
+  int nr;                    /* number of reaction parameters (1..3)                            */
+  int flag_reaction_inv;     /* OptimizerSettings::flag_reaction_inv_: no Phi apply, rho grad   */
+  int diffusivity_inversion; /* OptimizerSettings::diffusivity_inversion_: kappa from x, grad   */
+  int regularization_norm;   /* 0 = L2 (on Phi p), 1 = L2b (on p)                              */
+  double beta;               /* OptimizerSettings::beta_                                        */
+  double k_scale;            /* OptimizerSettings::k_scale_ (x entries are multiplied by it)    */
+  double rho_scale;          /* OptimizerSettings::rho_scale_                                   */
+  int phi_store;             /* TumorParameters::phi_store_: stored-Phi gradient formula        */
+  int all_gradients;         /* extension: p, kappa and rho gradients from one sweep            */
+} glia_opt_settings;
+
+/* Counters (TumorStatistics, include/utils/Utils.h:43-96, and PdeOperators::diff_ksp_itr_*). */
+typedef struct glia_stats {
+  int64_t nb_state_solves;
+  int64_t nb_adjoint_solves;
+  int64_t nb_obj_evals;
+  int64_t nb_grad_evals;
+  int64_t diff_ksp_itr_state; /* PCG iterations accumulated over the last solveState          */
+  int64_t diff_ksp_itr_adj;   /* PCG iterations accumulated over the last solveAdjoint        */
+  int64_t total_diffusion_solves;
+  int64_t total_pcg_iterations;
+  int64_t total_fft_execs; /* 3-D transforms executed (a batch of b counts b)               */
+  int last_ksp_itr;        /* DiffusionSolver::ksp_itr_ of the last solve                   */
+  int max_ksp_itr;
+  double last_rnorm; /* final preconditioned residual norm of the last solve              */
+} glia_stats;
+
+/* ---- lifecycle ----------------------------------------------------------------------------- */
+/* initializeGrid(n, params, spec_ops) + SpectralOperators::setup
+ * (src/grad/SpectralOperators.cpp:19-66, 424-446). n must be even, 8 <= n <= 1024. */
+int glia_create(int n, int precision, int engine, glia_ctx** out);
+int glia_destroy(glia_ctx* ctx);
+const char* glia_last_error(const glia_ctx* ctx);
+const char* glia_version(void);
+int glia_set_pointer_mode(glia_ctx* ctx, int mode);
+int glia_set_stream(glia_ctx* ctx, void* cuda_stream); /* NULL = the context's own stream */
+int glia_synchronize(glia_ctx* ctx);
+/* Device bytes currently held by the context (fields, spectra, history, plans). */
+int glia_device_bytes(const glia_ctx* ctx, int64_t* bytes);
+
+/* ---- parameters ---------------------------------------------------------------------------- */
+/* TumorParameters::dt_, nt_, order_ (include/Parameters.h:164-166, 226). Resizes the history
+ * like PdeOperatorsRD::resizeTimeHistory (src/pde/PdeOperators.cpp:57-103). */
+int glia_set_time(glia_ctx* ctx, double dt, int nt, int order);
+/* KSPSetTolerances(ksp_, 1e-6, default, default, 5000) (src/pde/DiffusionSolver.cpp:27). */
+int glia_set_pcg(glia_ctx* ctx, double rtol, int maxit, int pc_dt_mode, double pc_dt);
+/* TumorParameters::adjoint_store_ / time_history_off_ plus the checkpoint extension. */
+int glia_set_history(glia_ctx* ctx, int mode, int checkpoint_every, int adjoint_store);
+int glia_set_opt(glia_ctx* ctx, const glia_opt_settings* s);
+
+/* ---- material properties and coefficients -------------------------------------------------- */
+/* MatProp::setValuesCustom (src/mat/MatProp.cpp:134-203): NULL maps are zero; clip >= 0,
+ * bg = 1 - sum, filter = [(wm > 0.1 or gm > 0.1) and vt < 0.8]. */
+int glia_set_tissue(glia_ctx* ctx, const void* wm, const void* gm, const void* csf, const void* vt);
+/* MatProp::setValuesSinusoidal (src/mat/MatProp.cpp:34-68). */
+int glia_set_tissue_sinusoidal(glia_ctx* ctx);
+/* DiffCoef::setValues (src/mat/DiffCoef.cpp:77-132) + ReacCoef::setValues
+ * (src/mat/ReacCoef.cpp:13-38) + DiffusionSolver::precFactor. */
+int glia_set_coefficients(glia_ctx* ctx, double k, double k_gm_wm, double k_glm_wm, double rho,
+                          double r_gm_wm, double r_glm_wm);
+/* DiffCoef::setValuesSinusoidal (src/mat/DiffCoef.cpp:134-187); does not refactor the PC. */
+int glia_set_diffusivity_sinusoidal(glia_ctx* ctx, double scale);
+/* DiffusionSolver::precFactor() (src/pde/DiffusionSolver.cpp:119-180). */
+int glia_prec_factor(glia_ctx* ctx);
+/* DiffusionSolver::solve(Vec c, dt) (src/pde/DiffusionSolver.cpp:217-250); c in/out. */
+int glia_diffusion_solve(glia_ctx* ctx, void* c, double dt, int* ksp_itr);
+/* DiffCoef::applyD(dc, c) (src/mat/DiffCoef.cpp:249-271). */
+int glia_apply_d(glia_ctx* ctx, const void* c, void* dc);
+/* SpectralOperators::weierstrassSmoother (src/grad/SpectralOperators.cpp:264-381). */
+int glia_smooth(glia_ctx* ctx, void* out, const void* in, double sigma);
+
+/* ---- Gaussian basis (Phi) ------------------------------------------------------------------ */
+/* Phi::phiMesh (src/mat/Phi.cpp:148-234): np lattice centres around cm, spacing = factor*sigma.
+ * Host-only helper; centers_out holds 3*np doubles. */
+int glia_phi_mesh(int np, const double cm[3], double sigma, double spacing_factor,
+                  double* centers_out);
+/* Phi::setGaussians (explicit centres) + Phi::setValues (src/mat/Phi.cpp:33-144): each basis
+ * function is trunc_5sigma(W_smooth * (filter * gaussian)); normalised by the global max.
+ * Requires tissue. smoothing_factor: sigma_smooth = factor * 2*pi/n. */
+int glia_set_phi(glia_ctx* ctx, const double* centers, int np, double sigma,
+                 double smoothing_factor);
+/* Phi::apply (src/mat/Phi.cpp:313-377): c0 = Phi p. */
+int glia_phi_apply(glia_ctx* ctx, const double* p, void* c0);
+/* Phi::applyTranspose (src/mat/Phi.cpp:379-439): pout = Phi^T v. */
+int glia_phi_apply_transpose(glia_ctx* ctx, const void* v, double* pout);
+
+/* ---- observation operator ------------------------------------------------------------------ */
+/* Obs::setDefaultFilter (src/mat/Obs.cpp:26-55): filter = [data > thr]. */
+int glia_set_obs_threshold(glia_ctx* ctx, const void* data, double thr);
+/* Obs::setCustomFilter (src/mat/Obs.cpp:57-69). */
+int glia_set_obs_filter(glia_ctx* ctx, const void* filter);
+
+/* ---- PDE operators --------------------------------------------------------------------------- */
+/* Tumor::c_0_ (used by the derivative operators when flag_reaction_inv is set). */
+int glia_set_c0(glia_ctx* ctx, const void* c0);
+/* PdeOperatorsRD::solveState(int linearized) (src/pde/PdeOperators.cpp:235-316).
+ * c0 may be NULL (use Tumor::c_0_); c1 may be NULL. linearized: 0 only in this version. */
+int glia_solve_state(glia_ctx* ctx, int linearized, const void* c0, void* c1);
+/* PdeOperatorsRD::solveAdjoint(int linearized) (src/pde/PdeOperators.cpp:372-420).
+ * Needs a preceding glia_solve_state. a0 may be NULL. */
+int glia_solve_adjoint(glia_ctx* ctx, int linearized, const void* pt, void* a0);
+/* PdeOperatorsRD::c_[i] (FULL history only) / p_[i] (after an adjoint, FULL history only). */
+int glia_get_state(glia_ctx* ctx, int i, void* out);
+int glia_get_adjoint(glia_ctx* ctx, int i, void* out);
+
+/* ---- derivative operators -------------------------------------------------------------------- */
+/* DerivativeOperatorsRD::evaluateObjective (src/grad/DerivativeOperatorsRD.cpp:7-61).
+ * x = [p (np), kappa (nk), rho (nr)], d1 = data at t = 1 (grid field). */
+int glia_eval_objective(glia_ctx* ctx, const double* x, int nx, const void* d1, double* J);
+/* DerivativeOperatorsRD::evaluateGradient (src/grad/DerivativeOperatorsRD.cpp:63-127). */
+int glia_eval_gradient(glia_ctx* ctx, const double* x, int nx, const void* d1, double* dJ);
+/* DerivativeOperatorsRD::evaluateObjectiveAndGradient
+ * (src/grad/DerivativeOperatorsRD.cpp:130-226). */
+int glia_eval_objective_and_gradient(glia_ctx* ctx, const double* x, int nx, const void* d1,
+                                     double* J, double* dJ);
+
+int glia_get_stats(const glia_ctx* ctx, glia_stats* st);
+int glia_reset_stats(glia_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GLIA_RD_H_ */
