@@ -1,0 +1,1322 @@
+// engine_impl.cuh — host driver of the reaction–diffusion path on one GPU (one CUDA stream).
+//
+// Engine<R> implements, for storage type R (float: mixed path with FP64 reductions; double:
+// FP64), the reference's Tumor / MatProp / DiffCoef / ReacCoef / Phi / Obs / DiffusionSolver /
+// PdeOperatorsRD / DerivativeOperatorsRD state for one grid. Two diffusion-solve engines:
+//  - fused (default): the PCG of DiffusionSolver::solve runs in spectral space. x, r, p, w are
+//    half spectra; z = P r is never formed; the operator apply is 6 transforms
+//    (1 batched C2R of the three gradient spectra, 1 batched R2C of k * grad) plus 4 fused
+//    passes; the set-up reuses one D apply for both the right-hand side and r0.
+//  - reference-structured (GLIA_ENGINE_REFERENCE): a restatement of the reference's GPU
+//    structure with our own kernels: real-space PCG, 10 transforms per D apply, one kernel per
+//    PETSc vector operation and a host round trip per inner product. It is the plain baseline.
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <type_traits>
+#include <unordered_map>
+#include <vector>
+
+#include "engine.hpp"
+#include "kernels.cuh"
+
+namespace glia {
+
+static __global__ void k_solve_config(DevScalars* s, double a_cn, double pc_c, double rtol,
+                               double abstol, double divtol, int maxit, double kdot_weight) {
+  s->a_cn = a_cn;
+  s->pc_c = pc_c;
+  s->rtol = rtol;
+  s->abstol = abstol;
+  s->divtol = divtol;
+  s->maxit = maxit;
+  s->kdot_weight = kdot_weight;
+  s->status = 0;
+  s->it = 0;
+  s->iter = 0;
+}
+static __global__ void k_acc_reset(DevScalars* s) {
+  for (int q = 0; q < 8; q++) s->acc[q] = 0.0;
+}
+
+// Status summary read back after each PCG iteration (one 32-byte copy).
+struct SolveStatus {
+  int status, it;
+  double dp;
+};
+
+template <typename R>
+class Engine final : public EngineBase {
+ public:
+  Engine(int n, bool refmode) : g_(n), ref_(refmode) {
+    int dev = 0;
+    GLIA_CUDA(cudaGetDevice(&dev));
+    GLIA_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
+    GLIA_CUDA(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking));
+    stream_ = own_stream_;
+    red_blocks_ = sms_ * 4;
+    pw_blocks_ = sms_ * 8;
+    N_ = g_.N;
+    Ns_ = g_.Ns;
+    sc_ = dalloc<DevScalars>(1);
+    GLIA_CUDA(cudaMemsetAsync(sc_, 0, sizeof(DevScalars), stream_));
+    GLIA_CUDA(cudaMallocHost(&hsc_, sizeof(DevScalars)));
+    GLIA_CUDA(cudaMallocHost(&hst_, sizeof(SolveStatus)));
+    ws_.partials = dalloc<double>((int64_t)red_blocks_ * 4);
+    ws_.counter = dalloc<unsigned int>(1);
+    GLIA_CUDA(cudaMemsetAsync(ws_.counter, 0, sizeof(unsigned int), stream_));
+    for (R** f : {&wm_, &gm_, &csf_, &vt_, &bg_, &filter_, &kxx_, &rho_, &obs_, &c0_, &ct_, &p0_,
+                  &pt_, &tmp_})
+      *f = fld();
+    // MatProp::setValues defaults (src/mat/MatProp.cpp:20-33): wm = 1, filter = 1
+    fill(wm_, 1.0);
+    fill(filter_, 1.0);
+    fill(obs_, 1.0);
+    filter_sum_ = (double)N_;
+    chat_ = spec();
+    xhat_ = spec();
+    g3s_ = dalloc<R>(3 * Ns_ * 2);
+    g3r_ = dalloc<R>(3 * N_);
+    if (!ref_) {
+      rhat_ = spec();
+      phat_ = spec();
+      what_ = spec();
+    } else {
+      for (auto& t : t_) t = fld();
+      for (R** f : {&rb_, &rr_, &rz_, &rp_, &rw_, &rt2_, &kxy_, &kxz_, &kyz_, &kyy_, &kzz_})
+        *f = fld();
+      wh_ = spec();
+      pf_ = dalloc<R>(Ns_);
+    }
+    make_plans();
+    GLIA_CUDA(cudaStreamSynchronize(stream_));
+  }
+
+  ~Engine() override {
+    cudaStreamSynchronize(stream_);
+    for (cufftHandle* p : {&r2c1_, &c2r1_, &r2c3_, &c2r3_})
+      if (*p) cufftDestroy(*p);
+    destroy_batch_plans();
+    for (auto& kv : sizes_) cudaFree(kv.first);
+    if (hsc_) cudaFreeHost(hsc_);
+    if (hst_) cudaFreeHost(hst_);
+    if (own_stream_) cudaStreamDestroy(own_stream_);
+  }
+
+  // ------------------------------------------------------------------------------------------
+  // configuration
+  // ------------------------------------------------------------------------------------------
+  void set_pointer_mode(int mode) override {
+    if (mode < GLIA_PTR_HOST_F64 || mode > GLIA_PTR_DEVICE_F32)
+      throw Error(GLIA_ERR_INVALID, "unknown pointer mode");
+    ptr_mode_ = mode;
+  }
+  void set_stream(void* s) override {
+    stream_ = s ? (cudaStream_t)s : own_stream_;
+    for (cufftHandle p : {r2c1_, c2r1_, r2c3_, c2r3_}) GLIA_CUFFT(cufftSetStream(p, stream_));
+  }
+  void synchronize() override { GLIA_CUDA(cudaStreamSynchronize(stream_)); }
+  int64_t device_bytes() const override { return bytes_; }
+
+  void set_time(double dt, int nt, int order) override {
+    if (!(dt > 0) || nt < 1 || (order != 1 && order != 2))
+      throw Error(GLIA_ERR_INVALID, "set_time: need dt > 0, nt >= 1, order 1 or 2");
+    dt_ = dt;
+    nt_ = nt;
+    order_ = order;
+    ctx_dt_ = dt;  // a freshly built DiffusionSolver starts from TumorParameters::dt_
+    state_done_ = adjoint_done_ = false;
+    release_history();
+  }
+  void set_pcg(double rtol, int maxit, int pc_dt_mode, double pc_dt) override {
+    if (!(rtol > 0) || maxit < 1 || pc_dt_mode < 0 || pc_dt_mode > 2)
+      throw Error(GLIA_ERR_INVALID, "set_pcg: bad arguments");
+    rtol_ = rtol;
+    maxit_ = maxit;
+    pc_dt_mode_ = pc_dt_mode;
+    pc_dt_fixed_ = pc_dt;
+  }
+  void set_history(int mode, int every, int adjoint_store) override {
+    if (mode != GLIA_HISTORY_FULL && mode != GLIA_HISTORY_CHECKPOINT)
+      throw Error(GLIA_ERR_INVALID, "set_history: unknown mode");
+    if (mode == GLIA_HISTORY_CHECKPOINT && (every < 1 || ref_))
+      throw Error(GLIA_ERR_INVALID,
+                  "set_history: checkpointing needs every >= 1 and the fused engine");
+    hist_mode_ = mode;
+    every_ = every;
+    adjoint_store_ = adjoint_store != 0;
+    state_done_ = adjoint_done_ = false;
+    release_history();
+  }
+  void set_opt(const glia_opt_settings& s) override {
+    if (s.np < 0 || s.nk < 1 || s.nk > 3 || s.nr < 1 || s.nr > 3)
+      throw Error(GLIA_ERR_INVALID, "set_opt: need np >= 0, 1 <= nk, nr <= 3");
+    opt_ = s;
+  }
+
+  // ------------------------------------------------------------------------------------------
+  // material properties, coefficients, preconditioner
+  // ------------------------------------------------------------------------------------------
+  void set_tissue(const void* wm, const void* gm, const void* csf, const void* vt) override {
+    R* dst[4] = {wm_, gm_, csf_, vt_};
+    const void* src[4] = {wm, gm, csf, vt};
+    for (int i = 0; i < 4; i++) {
+      if (src[i])
+        import_field(src[i], dst[i]);
+      else
+        GLIA_CUDA(cudaMemsetAsync(dst[i], 0, N_ * sizeof(R), stream_));
+    }
+    k_matprop<R><<<red_blocks_, kThreads, 0, stream_>>>(N_, wm_, gm_, csf_, vt_, bg_, filter_,
+                                                         sc_, 0, ws_);
+    GLIA_LAUNCH_CHECK();
+    filter_sum_ = read_red(0);
+    tissue_set_ = true;
+  }
+  void set_tissue_sinusoidal() override {
+    k_sinusoid<R><<<red_blocks_, kThreads, 0, stream_>>>(g_, wm_, gm_, csf_, vt_, bg_, filter_,
+                                                          nullptr, 0.0, sc_, 0, ws_);
+    GLIA_LAUNCH_CHECK();
+    filter_sum_ = (double)N_;
+    tissue_set_ = true;
+  }
+  // DiffCoef::setValues (src/mat/DiffCoef.cpp:77-132)
+  void diffcoef_set(double ks, double kgm, double kglm) {
+    k_scale_ = ks;
+    k_gm_wm_ = kgm;
+    k_glm_wm_ = kglm;
+    double dgm = ks * kgm, dwm = ks, dglm = ks * kglm;
+    dgm = (dgm <= 0) ? 0.0 : dgm;
+    dglm = (dglm <= 0) ? 0.0 : dglm;
+    k_assemble<R><<<red_blocks_, kThreads, 0, stream_>>>(N_, kxx_, wm_, gm_, csf_, dwm, dgm,
+                                                          dglm, sc_, 0, ws_);
+    GLIA_LAUNCH_CHECK();
+    const double ksum = read_red(0);
+    // filter sum: MatProp filter (src/mat/DiffCoef.cpp:109)
+    kxx_avg_ = ksum * (1.0 / filter_sum_);
+    kxx_sinusoidal_ = false;
+    if (ref_) ref_copy_k();
+  }
+  // ReacCoef::setValues (src/mat/ReacCoef.cpp:13-38)
+  void reaccoef_set(double rs, double rgm, double rglm) {
+    rho_scale_ = rs;
+    r_gm_wm_ = rgm;
+    r_glm_wm_ = rglm;
+    double dgm = rs * rgm, dwm = rs, dglm = rs * rglm;
+    dgm = (dgm <= 0) ? 0.0 : dgm;
+    dglm = (dglm <= 0) ? 0.0 : dglm;
+    k_assemble<R><<<red_blocks_, kThreads, 0, stream_>>>(N_, rho_, wm_, gm_, csf_, dwm, dgm,
+                                                          dglm, sc_, 1, ws_);
+    GLIA_LAUNCH_CHECK();
+  }
+  void set_coefficients(double k, double kgm, double kglm, double rho, double rgm,
+                        double rglm) override {
+    diffcoef_set(k, kgm, kglm);
+    reaccoef_set(rho, rgm, rglm);
+    prec_factor();
+  }
+  void set_diffusivity_sinusoidal(double scale) override {
+    k_scale_ = scale;
+    k_sinusoid<R><<<red_blocks_, kThreads, 0, stream_>>>(g_, nullptr, nullptr, nullptr, nullptr,
+                                                          nullptr, nullptr, kxx_, scale, sc_, 0,
+                                                          ws_);
+    GLIA_LAUNCH_CHECK();
+    kxx_avg_ = read_red(0) * (1.0 / (double)N_);
+    kxx_sinusoidal_ = true;
+    if (ref_) ref_copy_k();
+  }
+  double pc_dt_now() const { return pc_dt_mode_ == GLIA_PC_DT_FIXED ? pc_dt_fixed_ : ctx_dt_; }
+  // DiffusionSolver::precFactor (src/pde/DiffusionSolver.cpp:119-180): the preconditioner is the
+  // pair (kbar, dt_pc) captured now; the fused path evaluates it from wave numbers on the fly.
+  void prec_factor_dt(double dtpc) {
+    pc_kbar_ = kxx_avg_;
+    pc_dt_ = dtpc;
+    if (ref_) {
+      k_precfactor<R><<<pw_blocks_, kThreads, 0, stream_>>>(g_, pf_, dtpc, kxx_avg_);
+      GLIA_LAUNCH_CHECK();
+    }
+  }
+  void prec_factor() override { prec_factor_dt(pc_dt_now()); }
+
+  // ------------------------------------------------------------------------------------------
+  // diffusion solve
+  // ------------------------------------------------------------------------------------------
+  int diffusion_solve(void* c, double dt) override {
+    if (!(dt > 0)) throw Error(GLIA_ERR_INVALID, "diffusion_solve: dt must be > 0");
+    import_field(c, tmp_);
+    solve(tmp_, dt, nullptr, nullptr, 0.0);
+    export_field(tmp_, c);
+    return ksp_itr_;
+  }
+
+  // DiffusionSolver::solve (src/pde/DiffusionSolver.cpp:217-250). chat_slot receives F(c) (the
+  // state spectrum, kept for the kappa gradient); cx/kdot_w add kdot_w * <cx, D c> to acc[6].
+  void solve(R* c, double dts, R* chat_slot, const R* cx, double kdot_w) {
+    ctx_dt_ = dts;
+    if (pc_dt_mode_ == GLIA_PC_DT_MATCHED) prec_factor_dt(2.0 * dts);
+    st_.total_diffusion_solves++;
+    if (k_scale_ == 0) {
+      ksp_itr_ = 0;
+      if (chat_slot) r2c(r2c1_, c, chat_slot);
+      return;
+    }
+    if (ref_)
+      ref_solve(c, dts);
+    else
+      fused_solve(c, dts, chat_slot ? chat_slot : chat_, cx, kdot_w);
+  }
+
+  void fused_solve(R* c, double dts, R* chat, const R* cx, double kdot_w) {
+    k_solve_config<<<1, 1, 0, stream_>>>(sc_, 0.5 * dts, 0.25 * pc_dt_ * pc_kbar_, rtol_, abstol_,
+                                         divtol_, maxit_, kdot_w);
+    GLIA_LAUNCH_CHECK();
+    // set-up: chat = F c; D c; b = c + a D c; r0 = 2 a D c; x0 = c; n = 0 convergence test
+    r2c(r2c1_, c, chat);
+    launch_grad3<false>(chat, nullptr);
+    apply_k_spectral();
+    k_spec_div<R, EPI_SETUP><<<red_blocks_, kThreads, 0, stream_>>>(g_, g3s_, chat, cx, xhat_,
+                                                                     rhat_, R(0), sc_, ws_);
+    GLIA_LAUNCH_CHECK();
+    SolveStatus s = read_status();
+    while (s.status == 0) {
+      launch_grad3<true>(rhat_, phat_);  // p = P r + b p, gradient spectra of p
+      apply_k_spectral();                // 3 C2R, k *, 3 R2C
+      k_spec_div<R, EPI_CGW><<<red_blocks_, kThreads, 0, stream_>>>(g_, g3s_, phat_, nullptr,
+                                                                     what_, nullptr, R(0), sc_, ws_);
+      GLIA_LAUNCH_CHECK();
+      k_cg_update<R><<<red_blocks_, kThreads, 0, stream_>>>(g_, xhat_, phat_, rhat_, what_, sc_,
+                                                            ws_);
+      GLIA_LAUNCH_CHECK();
+      s = read_status();
+    }
+    c2r(c2r1_, xhat_, c);  // x = F^-1 (x')
+    finish_solve(s);
+  }
+
+  template <bool CGDIR>
+  void launch_grad3(const R* src, R* pdir) {
+    k_spec_grad3<R, CGDIR><<<pw_blocks_, kThreads, 0, stream_>>>(g_, src, pdir, g3s_, sc_);
+    GLIA_LAUNCH_CHECK();
+  }
+  // gradient spectra (g3s_) -> real gradient -> times k -> spectra of k * grad (g3s_)
+  void apply_k_spectral() {
+    c2r(c2r3_, g3s_, g3r_, 3);
+    k_mul_k3<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, g3r_, kxx_, sc_, 0);
+    GLIA_LAUNCH_CHECK();
+    r2c(r2c3_, g3r_, g3s_, 3);
+  }
+
+  void finish_solve(const SolveStatus& s) {
+    ksp_itr_ = s.it;
+    st_.last_ksp_itr = s.it;
+    st_.max_ksp_itr = std::max(st_.max_ksp_itr, s.it);
+    st_.total_pcg_iterations += s.it;
+    st_.last_rnorm = s.dp;
+    if (s.status < 0) {
+      const char* why = s.status == -3   ? "maximum iterations"
+                        : s.status == -4 ? "divergence tolerance"
+                        : s.status == -8 ? "indefinite operator"
+                                         : "NaN or Inf residual";
+      throw Error(GLIA_ERR_NOT_CONVERGED, std::string("diffusion PCG stopped: ") + why +
+                                              " after " + std::to_string(s.it) + " iterations");
+    }
+  }
+
+  // ---- reference-structured path -----------------------------------------------------------
+  void ref_copy_k() {  // DiffCoef keeps kyy = kzz = kxx and zero off-diagonal fields
+    GLIA_CUDA(cudaMemcpyAsync(kyy_, kxx_, N_ * sizeof(R), cudaMemcpyDeviceToDevice, stream_));
+    GLIA_CUDA(cudaMemcpyAsync(kzz_, kxx_, N_ * sizeof(R), cudaMemcpyDeviceToDevice, stream_));
+    for (R* f : {kxy_, kxz_, kyz_}) GLIA_CUDA(cudaMemsetAsync(f, 0, N_ * sizeof(R), stream_));
+  }
+  void vaxpy(R* y, double a, const R* x) {
+    k_axpy<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, y, a, x);
+    GLIA_LAUNCH_CHECK();
+  }
+  void vaypx(R* y, double b, const R* x) {
+    k_aypx<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, y, b, x);
+    GLIA_LAUNCH_CHECK();
+  }
+  void vmult(R* z, const R* x, const R* y) {
+    k_pointwise_mult<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, z, x, y);
+    GLIA_LAUNCH_CHECK();
+  }
+  void vcopy(R* y, const R* x) {
+    GLIA_CUDA(cudaMemcpyAsync(y, x, N_ * sizeof(R), cudaMemcpyDeviceToDevice, stream_));
+  }
+  void vzero(R* y) { GLIA_CUDA(cudaMemsetAsync(y, 0, N_ * sizeof(R), stream_)); }
+  double vdot(const R* x, const R* y) {  // PETSc VecDot: one reduction, scalar to the host
+    k_dot<R><<<red_blocks_, kThreads, 0, stream_>>>(N_, x, y, sc_, 0, ws_);
+    GLIA_LAUNCH_CHECK();
+    return read_red(0);
+  }
+  // SpectralOperators::computeGradient (src/grad/SpectralOperators.cpp:100-177)
+  void ref_gradient(R* gx, R* gy, R* gz, const R* x) {
+    r2c(r2c1_, x, xhat_);
+    R* out[3] = {gx, gy, gz};
+    for (int d = 0; d < 3; d++) {
+      k_mult_wavenumber<R><<<pw_blocks_, kThreads, 0, stream_>>>(g_, d, xhat_, wh_);
+      GLIA_LAUNCH_CHECK();
+      c2r(c2r1_, wh_, out[d]);
+    }
+  }
+  // SpectralOperators::computeDivergence (src/grad/SpectralOperators.cpp:179-261)
+  void ref_divergence(R* div, const R* dx, const R* dy, const R* dz) {
+    const R* in[3] = {dx, dz, dy};
+    const int dim[3] = {0, 2, 1};
+    for (int q = 0; q < 3; q++) {
+      r2c(r2c1_, in[q], xhat_);
+      k_mult_wavenumber<R><<<pw_blocks_, kThreads, 0, stream_>>>(g_, dim[q], xhat_, wh_);
+      GLIA_LAUNCH_CHECK();
+      c2r(c2r1_, wh_, q == 0 ? div : t_[7]);
+      if (q) vaxpy(div, 1.0, t_[7]);
+    }
+  }
+  // DiffCoef::applyD + applyK (src/mat/DiffCoef.cpp:206-271)
+  void ref_applyD(R* dc, const R* c) {
+    ref_gradient(t_[4], t_[5], t_[6], c);
+    for (int i = 1; i < 4; i++) vzero(t_[i]);
+    const R* K[3][3] = {{kxx_, kxy_, kxz_}, {kxy_, kyy_, kyz_}, {kxz_, kyz_, kzz_}};
+    for (int row = 0; row < 3; row++)
+      for (int col = 0; col < 3; col++) {
+        vmult(t_[0], K[row][col], t_[4 + col]);
+        vaxpy(t_[1 + row], 1.0, t_[0]);
+      }
+    ref_divergence(dc, t_[1], t_[2], t_[3]);
+  }
+  void ref_operatorA(R* y, const R* x) {  // operatorA (:97-117)
+    vcopy(y, x);
+    ref_applyD(rt2_, y);
+    vaxpy(y, -0.5 * ctx_dt_, rt2_);
+  }
+  void ref_applyPC(R* y, const R* x) {  // applyPC (:182-215)
+    vcopy(y, x);
+    r2c(r2c1_, y, xhat_);
+    k_hadamard_real<R><<<pw_blocks_, kThreads, 0, stream_>>>(Ns_, xhat_, pf_);
+    GLIA_LAUNCH_CHECK();
+    c2r(c2r1_, xhat_, y);
+  }
+  // KSPSolve_CG + KSPConvergedDefault with host scalars, as PETSc runs them
+  void ref_solve(R* c, double dts) {
+    vcopy(rb_, c);
+    ref_applyD(rt2_, rb_);
+    vaxpy(rb_, 0.5 * dts, rt2_);
+    ref_operatorA(rr_, c);
+    vaypx(rr_, -1.0, rb_);
+    ref_applyPC(rz_, rr_);
+    double dp = std::sqrt(vdot(rz_, rz_));
+    ref_applyPC(rw_, rb_);
+    double snorm = std::sqrt(vdot(rw_, rw_));
+    if (snorm == 0) snorm = dp;
+    const double rnorm0 = snorm, ttol = std::max(rtol_ * rnorm0, abstol_);
+    auto conv = [&](double rn) {
+      if (std::isnan(rn) || std::isinf(rn)) return -9;
+      if (rn <= ttol) return 1;
+      if (rn >= divtol_ * rnorm0) return -4;
+      return 0;
+    };
+    int reason = conv(dp), its = 0;
+    if (reason == 0) {
+      double beta = vdot(rz_, rr_), betaold = 0, dpi = 0, dpiold = 0;
+      int i = 0;
+      do {
+        its = i + 1;
+        if (beta == 0.0) {
+          reason = 2;
+          break;
+        }
+        if (i == 0)
+          vcopy(rp_, rz_);
+        else
+          vaypx(rp_, beta / betaold, rz_);
+        dpiold = dpi;
+        ref_operatorA(rw_, rp_);
+        dpi = vdot(rp_, rw_);
+        betaold = beta;
+        if (dpi == 0.0 || (i > 0 && dpi * dpiold <= 0.0)) {
+          reason = -8;
+          break;
+        }
+        const double a = beta / dpi;
+        vaxpy(c, a, rp_);
+        vaxpy(rr_, -a, rw_);
+        ref_applyPC(rz_, rr_);
+        dp = std::sqrt(vdot(rz_, rz_));
+        reason = conv(dp);
+        if (reason) break;
+        beta = vdot(rz_, rr_);
+        i++;
+      } while (i < maxit_);
+      if (i >= maxit_ && reason == 0) reason = -3;
+    }
+    finish_solve(SolveStatus{reason < 0 ? reason : 0, its, dp});
+  }
+
+  // ------------------------------------------------------------------------------------------
+  // D apply and smoother
+  // ------------------------------------------------------------------------------------------
+  void applyD_into(R* dc, const R* c) {
+    if (ref_) {
+      ref_applyD(dc, c);
+      return;
+    }
+    r2c(r2c1_, c, chat_);
+    launch_grad3<false>(chat_, nullptr);
+    apply_k_spectral();
+    k_spec_div<R, EPI_APPLYD><<<pw_blocks_, kThreads, 0, stream_>>>(
+        g_, g3s_, nullptr, nullptr, xhat_, nullptr, (R)g_.invN, sc_, ws_);
+    GLIA_LAUNCH_CHECK();
+    c2r(c2r1_, xhat_, dc);
+  }
+  void apply_d(const void* c, void* dc) override {
+    import_field(c, tmp_);
+    applyD_into(p0_, tmp_);
+    export_field(p0_, dc);
+  }
+  // spectrum of the normalised Weierstrass kernel for sigma, times h^3 / N
+  // (SpectralOperators::weierstrassSmoother, src/grad/SpectralOperators.cpp:264-381)
+  const R* smoother_kernel(double sigma) {
+    if (wkern_ && wkern_sigma_ == sigma) return wkern_;
+    if (!wkern_) wkern_ = spec();
+    R* f = g3r_;
+    k_weierstrass<R><<<red_blocks_, kThreads, 0, stream_>>>(g_, f, sigma, sc_, 0, ws_);
+    GLIA_LAUNCH_CHECK();
+    const double sum_f = read_red(0);
+    const double h = 2.0 * M_PI / g_.n, h3 = h * h * h;
+    k_scale<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, f, 1.0 / (sum_f * h3));
+    GLIA_LAUNCH_CHECK();
+    r2c(r2c1_, f, wkern_);
+    k_scale<R><<<pw_blocks_, kThreads, 0, stream_>>>(2 * Ns_, wkern_, g_.invN * h3);
+    GLIA_LAUNCH_CHECK();
+    wkern_sigma_ = sigma;
+    return wkern_;
+  }
+  void smooth_into(R* out, const R* in, double sigma) {
+    if (sigma == 0) {
+      if (out != in) vcopy(out, in);
+      return;
+    }
+    const R* K = smoother_kernel(sigma);
+    r2c(r2c1_, in, chat_);
+    k_spec_mul<R><<<pw_blocks_, kThreads, 0, stream_>>>(Ns_, 1, chat_, K);
+    GLIA_LAUNCH_CHECK();
+    c2r(c2r1_, chat_, out);
+  }
+  void smooth(void* out, const void* in, double sigma) override {
+    import_field(in, tmp_);
+    smooth_into(tmp_, tmp_, sigma);
+    export_field(tmp_, out);
+  }
+
+  // ------------------------------------------------------------------------------------------
+  // Phi
+  // ------------------------------------------------------------------------------------------
+  void set_phi(const double* centers, int np, double sigma, double smoothing_factor) override {
+    if (np < 1 || !(sigma > 0)) throw Error(GLIA_ERR_INVALID, "set_phi: need np >= 1, sigma > 0");
+    phi_np_ = np;
+    phi_sigma_ = sigma;
+    centers_.assign(centers, centers + 3 * np);
+    // boxes [centre - 5 sigma, centre + 5 sigma] clipped to the grid (non-periodic distances)
+    const double h = 2.0 * M_PI / g_.n;
+    std::vector<PhiBox> boxes(np);
+    int64_t off = 0;
+    for (int i = 0; i < np; i++) {
+      for (int d = 0; d < 3; d++) {
+        const double a = (centers[3 * i + d] - 5.0 * sigma) / h;
+        const double b = (centers[3 * i + d] + 5.0 * sigma) / h;
+        int l = (int)std::ceil(a - 1e-9), u = (int)std::floor(b + 1e-9);
+        l = std::max(l, 0);
+        u = std::min(u, g_.n - 1);
+        boxes[i].lo[d] = l;
+        boxes[i].ext[d] = std::max(0, u - l + 1);
+      }
+      boxes[i].off = off;
+      off += (int64_t)boxes[i].ext[0] * boxes[i].ext[1] * boxes[i].ext[2];
+    }
+    phi_box_h_ = boxes;
+    if (phi_store_) dfree(phi_store_);
+    if (phi_boxes_) dfree(phi_boxes_);
+    if (phi_centers_) dfree(phi_centers_);
+    phi_store_ = dalloc<R>(std::max<int64_t>(off, 1));
+    phi_boxes_ = dalloc<PhiBox>(np);
+    phi_centers_ = dalloc<double>(3 * np);
+    GLIA_CUDA(cudaMemcpyAsync(phi_boxes_, boxes.data(), np * sizeof(PhiBox),
+                              cudaMemcpyHostToDevice, stream_));
+    GLIA_CUDA(cudaMemcpyAsync(phi_centers_, centers, 3 * np * sizeof(double),
+                              cudaMemcpyHostToDevice, stream_));
+    // Phi::setValues (stored mode, src/mat/Phi.cpp:96-130), B functions per batch
+    const int B = std::min(np, 8);
+    ensure_batch_plans(B);
+    R* full = dalloc<R>((int64_t)B * N_);
+    R* fsp = dalloc<R>((int64_t)B * Ns_ * 2);
+    GLIA_CUDA(cudaMemsetAsync(full, 0, (size_t)B * N_ * sizeof(R), stream_));
+    const int xb = 8;
+    double* bmax = dalloc<double>((int64_t)B * xb);
+    std::vector<double> hmax((size_t)B * xb);
+    const R* K = smoother_kernel(smoothing_factor * 2.0 * M_PI / g_.n);
+    phi_max_each_.assign(np, 0.0);
+    for (int b0 = 0; b0 < np; b0 += B) {
+      const int nb = std::min(B, np - b0);
+      k_phi_gauss<R><<<pw_blocks_, kThreads, 0, stream_>>>(g_, nb, phi_centers_ + 3 * b0, sigma,
+                                                            filter_, full);
+      GLIA_LAUNCH_CHECK();
+      r2c(r2cB_, full, fsp, B);
+      k_spec_mul<R><<<pw_blocks_, kThreads, 0, stream_>>>(Ns_, nb, fsp, K);
+      GLIA_LAUNCH_CHECK();
+      c2r(c2rB_, fsp, full, B);
+      dim3 grid(xb, nb);
+      k_phi_extract<R><<<grid, kThreads, 0, stream_>>>(g_, nb, full, phi_boxes_ + b0,
+                                                        phi_centers_ + 3 * b0, sigma, phi_store_,
+                                                        bmax);
+      GLIA_LAUNCH_CHECK();
+      GLIA_CUDA(cudaMemcpyAsync(hmax.data(), bmax, (size_t)nb * xb * sizeof(double),
+                                cudaMemcpyDeviceToHost, stream_));
+      GLIA_CUDA(cudaStreamSynchronize(stream_));
+      for (int b = 0; b < nb; b++) {
+        double m = 0.0;
+        for (int q = 0; q < xb; q++) m = std::max(m, hmax[(size_t)b * xb + q]);
+        phi_max_each_[b0 + b] = m;
+      }
+    }
+    dfree(full);
+    dfree(fsp);
+    dfree(bmax);
+    destroy_batch_plans();
+    // cell lists for the gathered apply
+    const int cpd = (g_.n + 7) / 8;
+    std::vector<std::vector<int>> lists((size_t)cpd * cpd * cpd);
+    for (int i = 0; i < np; i++) {
+      const PhiBox& bx = boxes[i];
+      if (bx.ext[0] == 0 || bx.ext[1] == 0 || bx.ext[2] == 0) continue;
+      int c0[3], c1[3];
+      for (int d = 0; d < 3; d++) {
+        c0[d] = bx.lo[d] / 8;
+        c1[d] = (bx.lo[d] + bx.ext[d] - 1) / 8;
+      }
+      for (int a = c0[0]; a <= c1[0]; a++)
+        for (int b = c0[1]; b <= c1[1]; b++)
+          for (int c = c0[2]; c <= c1[2]; c++) lists[((size_t)a * cpd + b) * cpd + c].push_back(i);
+    }
+    std::vector<int> ptr(lists.size() + 1, 0), flat;
+    for (size_t k = 0; k < lists.size(); k++) {
+      ptr[k + 1] = ptr[k] + (int)lists[k].size();
+      flat.insert(flat.end(), lists[k].begin(), lists[k].end());
+    }
+    if (cell_ptr_) dfree(cell_ptr_);
+    if (cell_list_) dfree(cell_list_);
+    if (phi_p_) dfree(phi_p_);
+    cell_ptr_ = dalloc<int>(ptr.size());
+    cell_list_ = dalloc<int>(std::max<size_t>(flat.size(), 1));
+    phi_p_ = dalloc<double>(np);
+    GLIA_CUDA(cudaMemcpyAsync(cell_ptr_, ptr.data(), ptr.size() * sizeof(int),
+                              cudaMemcpyHostToDevice, stream_));
+    if (!flat.empty())
+      GLIA_CUDA(cudaMemcpyAsync(cell_list_, flat.data(), flat.size() * sizeof(int),
+                                cudaMemcpyHostToDevice, stream_));
+    cells_per_dim_ = cpd;
+    GLIA_CUDA(cudaStreamSynchronize(stream_));
+  }
+  double phi_max_all() const {
+    double m = 0;
+    for (double v : phi_max_each_) m = std::max(m, v);
+    return m;
+  }
+  // Phi::apply (src/mat/Phi.cpp:313-377): stored mode scales by the global max, on-the-fly mode
+  // by the max over the active functions (1 when p has no non-zero).
+  void phi_apply_into(R* out, const double* p) {
+    if (phi_np_ < 1) throw Error(GLIA_ERR_STATE, "Phi is not set (glia_set_phi)");
+    double scale;
+    if (opt_.phi_store) {
+      scale = 1.0 / phi_max_all();
+    } else {
+      double pm = 0;
+      bool nnz = false;
+      for (int i = 0; i < phi_np_; i++)
+        if (p[i] != 0) {
+          nnz = true;
+          pm = std::max(pm, phi_max_each_[i]);
+        }
+      scale = 1.0 / (nnz ? pm : 1.0);
+    }
+    hphi_p_.assign(p, p + phi_np_);
+    GLIA_CUDA(cudaMemcpyAsync(phi_p_, hphi_p_.data(), phi_np_ * sizeof(double),
+                              cudaMemcpyHostToDevice, stream_));
+    const int cells = cells_per_dim_ * cells_per_dim_ * cells_per_dim_;
+    k_phi_apply<R><<<cells, 512, 0, stream_>>>(g_, cells_per_dim_, cell_ptr_, cell_list_,
+                                                phi_boxes_, phi_store_, phi_p_, scale, out);
+    GLIA_LAUNCH_CHECK();
+    GLIA_CUDA(cudaStreamSynchronize(stream_));  // hphi_p_ may be reused by the next call
+  }
+  void phi_applyT_from(const R* v, double* pout) {
+    if (phi_np_ < 1) throw Error(GLIA_ERR_STATE, "Phi is not set (glia_set_phi)");
+    k_phi_applyT<R><<<phi_np_, kThreads, 0, stream_>>>(g_, phi_boxes_, phi_store_, v, phi_p_);
+    GLIA_LAUNCH_CHECK();
+    GLIA_CUDA(cudaMemcpyAsync(pout, phi_p_, phi_np_ * sizeof(double), cudaMemcpyDeviceToHost,
+                              stream_));
+    GLIA_CUDA(cudaStreamSynchronize(stream_));
+    const double s = 1.0 / phi_max_all();
+    for (int i = 0; i < phi_np_; i++) pout[i] *= s;
+  }
+  void phi_apply(const double* p, void* c0) override {
+    phi_apply_into(tmp_, p);
+    export_field(tmp_, c0);
+  }
+  void phi_apply_transpose(const void* v, double* pout) override {
+    import_field(v, tmp_);
+    phi_applyT_from(tmp_, pout);
+  }
+
+  // ------------------------------------------------------------------------------------------
+  // observation operator, initial condition
+  // ------------------------------------------------------------------------------------------
+  void set_obs_threshold(const void* data, double thr) override {
+    import_field(data, tmp_);
+    k_threshold<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, tmp_, thr, obs_);
+    GLIA_LAUNCH_CHECK();
+  }
+  void set_obs_filter(const void* f) override { import_field(f, obs_); }
+  void set_c0(const void* c0) override { import_field(c0, c0_); }
+
+  // ------------------------------------------------------------------------------------------
+  // time history
+  // ------------------------------------------------------------------------------------------
+  void release_history() {
+    for (auto* v : {&c_hist_, &c_half_, &chat_hist_, &p_hist_, &ckpt_, &seg_c_, &seg_half_,
+                    &seg_chat_})
+      for (R*& f : *v) {
+        if (f) dfree(f);
+        f = nullptr;
+      }
+    for (auto* v : {&c_hist_, &c_half_, &chat_hist_, &p_hist_, &ckpt_, &seg_c_, &seg_half_,
+                    &seg_chat_})
+      v->clear();
+  }
+  bool full() const { return hist_mode_ == GLIA_HISTORY_FULL; }
+  // which gradient terms the next adjoint sweep accumulates
+  bool kappa_trick_ok() const {
+    return !ref_ && opt_.nk == 1 && k_scale_ > 0 && k_gm_wm_ >= 0 && k_glm_wm_ <= 0 &&
+           !kxx_sinusoidal_;
+  }
+  void ensure_history() {
+    const bool store_half = !ref_ || adjoint_store_;
+    if (full()) {
+      if ((int)c_hist_.size() != nt_ + 1) {
+        release_history();
+        c_hist_.resize(nt_ + 1);
+        p_hist_.resize(nt_ + 1);
+        for (auto& f : c_hist_) f = fld();
+        for (auto& f : p_hist_) f = fld();
+        if (store_half) {
+          c_half_.resize(nt_);
+          for (auto& f : c_half_) f = fld();
+        }
+        if (!ref_) {
+          chat_hist_.resize(nt_ + 1);
+          for (auto& f : chat_hist_) f = spec();
+        }
+      }
+    } else {
+      const int S = (nt_ + every_ - 1) / every_;
+      if ((int)ckpt_.size() != S) {
+        release_history();
+        ckpt_.resize(S);
+        for (auto& f : ckpt_) f = fld();
+        seg_c_.resize(every_ + 1);
+        seg_half_.resize(every_);
+        seg_chat_.resize(every_ + 1);
+        for (auto& f : seg_c_) f = fld();
+        for (auto& f : seg_half_) f = fld();
+        for (auto& f : seg_chat_) f = spec();
+      }
+    }
+  }
+
+  // One splitting step from the state in `c` (PdeOperatorsRD::solveState loop body,
+  // src/pde/PdeOperators.cpp:260-300). chat_slot: spectrum of c before the step; half_out:
+  // state after the first diffusion sub-step.
+  void step(R* c, R* chat_slot, R* half_out) {
+    if (order_ == 2) {
+      solve(c, dt_ / 2.0, chat_slot, nullptr, 0.0);
+      st_.diff_ksp_itr_state += ksp_itr_;
+      reaction(c, half_out);
+      solve(c, dt_ / 2.0, nullptr, nullptr, 0.0);
+      st_.diff_ksp_itr_state += ksp_itr_;
+    } else {
+      solve(c, dt_, chat_slot, nullptr, 0.0);
+      st_.diff_ksp_itr_state += ksp_itr_;
+      reaction(c, half_out);
+    }
+  }
+  void reaction(R* c, R* half_out) {
+    k_reaction_fwd<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, c, rho_, (R)dt_, half_out);
+    GLIA_LAUNCH_CHECK();
+  }
+
+  // PdeOperatorsRD::solveState(0) (src/pde/PdeOperators.cpp:235-316)
+  void solve_state_internal() {
+    st_.nb_state_solves++;
+    ensure_history();
+    st_.diff_ksp_itr_state = 0;
+    vcopy(ct_, c0_);
+    const bool trick = kappa_trick_ok();
+    if (full()) {
+      vcopy(c_hist_[0], ct_);
+      for (int i = 0; i < nt_; i++) {
+        R* half = c_half_.empty() ? nullptr : c_half_[i];
+        step(ct_, (!ref_ && trick) ? chat_hist_[i] : nullptr, half);
+        vcopy(c_hist_[i + 1], ct_);
+      }
+      if (!ref_ && trick) r2c(r2c1_, ct_, chat_hist_[nt_]);
+    } else {
+      for (int i = 0; i < nt_; i++) {
+        if (i % every_ == 0) vcopy(ckpt_[i / every_], ct_);
+        step(ct_, nullptr, nullptr);
+      }
+    }
+    state_done_ = true;
+    adjoint_done_ = false;
+    trick_at_state_ = trick;
+  }
+  void solve_state(const void* c0, void* c1) override {
+    if (c0) import_field(c0, c0_);
+    solve_state_internal();
+    if (c1) export_field(ct_, c1);
+  }
+
+  // adjoint step from alpha_{i+1} (in p0_) to alpha_i (PdeOperatorsRD::solveAdjoint body,
+  // :392-408); cx = F(c_{i+1}) adds w_{i+1} dt <c_{i+1}, D alpha_{i+1}> for the kappa gradient.
+  void adjoint_step(int i, const R* chalf, const R* cx, bool accumulate) {
+    const double w = (i + 1 == nt_) ? 0.5 : 1.0;
+    const R* cxx = accumulate ? cx : nullptr;
+    if (order_ == 2) {
+      solve(p0_, dt_ / 2.0, nullptr, cxx, w * dt_);
+      st_.diff_ksp_itr_adj += ksp_itr_;
+      reaction_adjoint(chalf);
+      solve(p0_, dt_ / 2.0, nullptr, nullptr, 0.0);
+      st_.diff_ksp_itr_adj += ksp_itr_;
+    } else {
+      solve(p0_, dt_, nullptr, cxx, w * dt_);
+      st_.diff_ksp_itr_adj += ksp_itr_;
+      reaction_adjoint(chalf);
+    }
+  }
+  void reaction_adjoint(const R* chalf) {
+    k_reaction_lin<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, p0_, rho_, chalf, (R)dt_);
+    GLIA_LAUNCH_CHECK();
+  }
+  // reactionAdjoint without stored half steps (src/pde/PdeOperators.cpp:331-344)
+  const R* recompute_half(const R* ci) {
+    vcopy(tmp_, ci);
+    solve(tmp_, order_ == 2 ? dt_ / 2.0 : dt_, nullptr, nullptr, 0.0);
+    st_.diff_ksp_itr_adj += ksp_itr_;
+    return tmp_;
+  }
+  // per-time-point gradient terms at time point i (state c_i, adjoint alpha_i in p0_)
+  void grad_point(int i, const R* ci, bool explicit_kappa) {
+    const double w = (i == 0 || i == nt_) ? 0.5 : 1.0;
+    k_grad_rho_acc<R><<<red_blocks_, kThreads, 0, stream_>>>(N_, ci, p0_, wm_, gm_, csf_, w * dt_,
+                                                              sc_, ws_);
+    GLIA_LAUNCH_CHECK();
+    if (explicit_kappa) {
+      R* gc = g3r_;
+      R* ga = ga3();
+      if (ref_) {  // computeGradient twice, as gradDiffusion does
+        ref_gradient(gc, gc + N_, gc + 2 * N_, ci);
+        ref_gradient(ga, ga + N_, ga + 2 * N_, p0_);
+      } else {
+        grad_real(ci, gc);
+        grad_real(p0_, ga);
+      }
+      k_grad_kappa_acc<R><<<red_blocks_, kThreads, 0, stream_>>>(N_, gc, ga, wm_, gm_, csf_,
+                                                                  w * dt_, sc_, ws_);
+      GLIA_LAUNCH_CHECK();
+    }
+  }
+  R* ga3() {
+    if (!ga3_) ga3_ = dalloc<R>(3 * N_);
+    return ga3_;
+  }
+  void grad_real(const R* x, R* out3) {  // spectral gradient into 3 real fields
+    r2c(r2c1_, x, chat_);
+    launch_grad3<false>(chat_, nullptr);
+    c2r(c2r3_, g3s_, out3, 3);
+  }
+
+  // PdeOperatorsRD::solveAdjoint(1) with the gradient time accumulation fused into the sweep.
+  void solve_adjoint_internal(bool accumulate) {
+    if (!state_done_) throw Error(GLIA_ERR_STATE, "solveAdjoint needs a preceding solveState");
+    st_.nb_adjoint_solves++;
+    st_.diff_ksp_itr_adj = 0;
+    vcopy(p0_, pt_);
+    const bool trick = trick_at_state_ && kappa_trick_ok();
+    const bool explicit_kappa = accumulate && !trick;
+    kappa_used_trick_ = trick;
+    if (accumulate) {
+      k_acc_reset<<<1, 1, 0, stream_>>>(sc_);
+      GLIA_LAUNCH_CHECK();
+    }
+    if (full()) {
+      vcopy(p_hist_[nt_], p0_);
+      if (accumulate && !ref_) grad_point(nt_, c_hist_[nt_], explicit_kappa);
+      for (int i = nt_ - 1; i >= 0; i--) {
+        const R* chalf = c_half_.empty() ? nullptr : c_half_[i];
+        if (order_ == 2) {
+          solve(p0_, dt_ / 2.0, nullptr, (accumulate && trick) ? chat_hist_[i + 1] : nullptr,
+                ((i + 1 == nt_) ? 0.5 : 1.0) * dt_);
+          st_.diff_ksp_itr_adj += ksp_itr_;
+          if (!chalf) chalf = recompute_half(c_hist_[i]);
+          reaction_adjoint(chalf);
+          solve(p0_, dt_ / 2.0, nullptr, nullptr, 0.0);
+          st_.diff_ksp_itr_adj += ksp_itr_;
+        } else {
+          solve(p0_, dt_, nullptr, (accumulate && trick) ? chat_hist_[i + 1] : nullptr,
+                ((i + 1 == nt_) ? 0.5 : 1.0) * dt_);
+          st_.diff_ksp_itr_adj += ksp_itr_;
+          if (!chalf) chalf = recompute_half(c_hist_[i]);
+          reaction_adjoint(chalf);
+        }
+        vcopy(p_hist_[i], p0_);
+        if (accumulate && !ref_) grad_point(i, c_hist_[i], explicit_kappa);
+      }
+      if (accumulate && trick) kappa_dot_at(chat_hist_[0], 0.5 * dt_);
+    } else {
+      // checkpointed: recompute each segment forward from its checkpoint, then sweep it back
+      const int S = (int)ckpt_.size();
+      if (accumulate) grad_point(nt_, ct_, explicit_kappa);
+      for (int s = S - 1; s >= 0; s--) {
+        const int i0 = s * every_, i1 = std::min(nt_, (s + 1) * every_);
+        vcopy(seg_c_[0], ckpt_[s]);
+        vcopy(tmp2(), ckpt_[s]);
+        for (int i = i0; i < i1; i++) {
+          const int64_t ks = st_.diff_ksp_itr_state;
+          step(tmp2(), trick ? seg_chat_[i - i0] : nullptr, seg_half_[i - i0]);
+          st_.diff_ksp_itr_state = ks;  // recompute solves are not state solves
+          vcopy(seg_c_[i - i0 + 1], tmp2());
+        }
+        if (trick) r2c(r2c1_, tmp2(), seg_chat_[i1 - i0]);
+        for (int i = i1 - 1; i >= i0; i--) {
+          adjoint_step(i, seg_half_[i - i0], trick ? seg_chat_[i - i0 + 1] : nullptr,
+                       accumulate && trick);
+          if (accumulate) grad_point(i, seg_c_[i - i0], explicit_kappa);
+        }
+        if (s == 0 && accumulate && trick) kappa_dot_at(seg_chat_[0], 0.5 * dt_);
+      }
+    }
+    adjoint_done_ = true;
+  }
+  R* tmp2() {
+    if (!tmp2_) tmp2_ = fld();
+    return tmp2_;
+  }
+  // acc[6] += w <c_0, D alpha_0>: a D apply on alpha_0 whose spectral epilogue takes the dot
+  void kappa_dot_at(const R* chat0, double w) {
+    k_solve_config<<<1, 1, 0, stream_>>>(sc_, 0.0, 0.0, rtol_, abstol_, divtol_, maxit_, w);
+    GLIA_LAUNCH_CHECK();
+    R* spec_a = xhat_;
+    r2c(r2c1_, p0_, spec_a);
+    launch_grad3<false>(spec_a, nullptr);
+    apply_k_spectral();
+    k_spec_div<R, EPI_SETUP><<<red_blocks_, kThreads, 0, stream_>>>(g_, g3s_, spec_a, chat0,
+                                                                     rhat_, what_, R(0), sc_, ws_);
+    GLIA_LAUNCH_CHECK();
+  }
+  void solve_adjoint(const void* pt, void* a0) override {
+    if (pt) import_field(pt, pt_);
+    solve_adjoint_internal(false);
+    if (a0) export_field(p0_, a0);
+  }
+  void get_state(int i, void* out) override {
+    if (!state_done_ || !full() || i < 0 || i > nt_)
+      throw Error(GLIA_ERR_STATE, "get_state: needs a state solve with full history, 0<=i<=nt");
+    export_field(c_hist_[i], out);
+  }
+  void get_adjoint(int i, void* out) override {
+    if (!adjoint_done_ || !full() || i < 0 || i > nt_)
+      throw Error(GLIA_ERR_STATE, "get_adjoint: needs an adjoint solve with full history");
+    export_field(p_hist_[i], out);
+  }
+
+  // ------------------------------------------------------------------------------------------
+  // derivative operators (src/grad/DerivativeOperatorsRD.cpp, DerivativeOperators.cpp)
+  // ------------------------------------------------------------------------------------------
+  bool update_kappa() const {
+    return opt_.diffusivity_inversion || opt_.flag_reaction_inv || opt_.all_gradients;
+  }
+  bool update_rho() const { return opt_.flag_reaction_inv || opt_.all_gradients; }
+  bool apply_phi() const { return !opt_.flag_reaction_inv || opt_.all_gradients; }
+  int nx() const { return opt_.np + opt_.nk + opt_.nr; }
+
+  // DerivativeOperators::updateReactionAndDiffusion (src/grad/DerivativeOperators.cpp:323-367)
+  void update_coefficients(const double* x) {
+    const int np = opt_.np, nk = opt_.nk, nr = opt_.nr;
+    if (update_kappa()) {
+      const double k1 = x[np] * opt_.k_scale;
+      const double k2 = nk > 1 ? x[np + 1] * opt_.k_scale : 0;
+      const double k3 = nk > 2 ? x[np + 2] * opt_.k_scale : 0;
+      // DiffCoef::updateIsotropicCoefficients (src/mat/DiffCoef.cpp:60-75)
+      diffcoef_set(k1, nk == 1 ? k_gm_wm_ : k2 / k1, nk == 1 ? k_glm_wm_ : k3 / k1);
+      prec_factor();
+    }
+    if (update_rho()) {
+      const double r1 = x[np + nk] * opt_.rho_scale;
+      const double r2 = nr > 1 ? x[np + nk + 1] * opt_.rho_scale : 0;
+      const double r3 = nr > 2 ? x[np + nk + 2] * opt_.rho_scale : 0;
+      reaccoef_set(r1, nr == 1 ? r_gm_wm_ : r2 / r1, nr == 1 ? r_glm_wm_ : r3 / r1);
+    }
+  }
+
+  void evaluate(const double* x, int nxin, const void* d1, double* J, double* dJ) override {
+    if (nxin != nx())
+      throw Error(GLIA_ERR_INVALID, "x has " + std::to_string(nxin) + " entries, expected " +
+                                        std::to_string(nx()) + " (np + nk + nr)");
+    const bool want_grad = dJ != nullptr;
+    if (J) st_.nb_obj_evals++;
+    if (want_grad) st_.nb_grad_evals++;
+    const int np = opt_.np, nk = opt_.nk, nr = opt_.nr;
+    if (want_grad) std::fill(dJ, dJ + nx(), 0.0);
+    R* data = d1_buf();
+    import_field(d1, data);
+    update_coefficients(x);
+    if (apply_phi()) phi_apply_into(c0_, x);
+    solve_state_internal();
+    const double h = 2.0 * M_PI / g_.n, h3 = h * h * h;
+    k_obs_residual<R><<<red_blocks_, kThreads, 0, stream_>>>(N_, ct_, obs_, data,
+                                                             want_grad ? pt_ : nullptr, sc_, ws_);
+    GLIA_LAUNCH_CHECK();
+    const double m1 = read_red(0);
+    if (want_grad) {
+      solve_adjoint_internal(true);
+      if (apply_phi()) p_gradient(x, dJ, h3);
+    }
+    double reg = 0;
+    if (opt_.regularization_norm == 0) {
+      if (opt_.beta != 0) reg = vdot_any(c0_, c0_) * 0.5 * opt_.beta * h3;
+    } else {
+      for (int i = 0; i < np; i++) reg += x[i] * x[i];
+      reg *= 0.5 * opt_.beta;
+    }
+    if (J) *J = h3 * 0.5 * m1 + reg;
+    if (!want_grad) return;
+    // gradDiffusion / gradReaction (src/grad/DerivativeOperators.cpp:189-321)
+    double acc[8];
+    if (ref_)
+      ref_time_integrals(acc);
+    else {
+      GLIA_CUDA(cudaMemcpyAsync(hsc_, sc_, sizeof(DevScalars), cudaMemcpyDeviceToHost, stream_));
+      GLIA_CUDA(cudaStreamSynchronize(stream_));
+      std::memcpy(acc, hsc_->acc, sizeof(acc));
+    }
+    if (update_kappa()) {
+      double Twm, Tgm, Tcsf;
+      if (!ref_ && kappa_used_trick_) {
+        // <m, grad c . grad a> = -<c, D a> / kappa with k = kappa (wm + k_gm_wm gm)
+        Twm = -acc[6] / k_scale_;
+        dJ[np] = Twm * h3;
+      } else {
+        Twm = acc[0];
+        Tgm = acc[1];
+        Tcsf = acc[2];
+        dJ[np] = Twm * h3;
+        if (nk == 1) dJ[np] += Tgm * h3 * k_gm_wm_;
+        if (nk > 1) dJ[np + 1] = Tgm * h3;
+        if (nk > 2) dJ[np + 2] = Tcsf * h3;
+      }
+    }
+    if (update_rho()) {
+      dJ[np + nk] = acc[3] * h3;
+      if (nr == 1) dJ[np + nk] += acc[4] * h3 * r_gm_wm_;
+      if (nr > 1) dJ[np + nk + 1] = acc[4] * h3;
+      if (nr > 2) dJ[np + nk + 2] = acc[5] * h3;
+    }
+  }
+  // p gradient (src/grad/DerivativeOperatorsRD.cpp:164-187)
+  void p_gradient(const double* x, double* dJ, double h3) {
+    const int np = opt_.np;
+    std::vector<double> tmpv(std::max(np, 1));
+    if (!opt_.phi_store) {
+      if (opt_.beta != 0) vaxpy_any(p0_, -opt_.beta, c0_);
+      phi_applyT_from(p0_, dJ);
+      for (int i = 0; i < np; i++) dJ[i] *= -h3;
+    } else {
+      phi_applyT_from(p0_, tmpv.data());
+      for (int i = 0; i < np; i++) tmpv[i] *= h3;
+      if (opt_.regularization_norm == 0) {
+        phi_applyT_from(c0_, dJ);
+        for (int i = 0; i < np; i++) dJ[i] = dJ[i] * opt_.beta * h3 - tmpv[i];
+      } else {
+        for (int i = 0; i < nx(); i++) dJ[i] = x[i] * opt_.beta - (i < np ? tmpv[i] : 0.0);
+      }
+    }
+  }
+  // reference-structured gradDiffusion / gradReaction over the stored history
+  void ref_time_integrals(double* acc) {
+    std::fill(acc, acc + 8, 0.0);
+    k_acc_reset<<<1, 1, 0, stream_>>>(sc_);
+    GLIA_LAUNCH_CHECK();
+    for (int i = 0; i <= nt_; i++) {
+      vcopy(p0_, p_hist_[i]);
+      grad_point(i, c_hist_[i], update_kappa());
+    }
+    GLIA_CUDA(cudaMemcpyAsync(hsc_, sc_, sizeof(DevScalars), cudaMemcpyDeviceToHost, stream_));
+    GLIA_CUDA(cudaStreamSynchronize(stream_));
+    std::memcpy(acc, hsc_->acc, 8 * sizeof(double));
+  }
+  double vdot_any(const R* x, const R* y) {
+    k_dot<R><<<red_blocks_, kThreads, 0, stream_>>>(N_, x, y, sc_, 0, ws_);
+    GLIA_LAUNCH_CHECK();
+    return read_red(0);
+  }
+  void vaxpy_any(R* y, double a, const R* x) {
+    k_axpy<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, y, a, x);
+    GLIA_LAUNCH_CHECK();
+  }
+  R* d1_buf() {
+    if (!d1_) d1_ = fld();
+    return d1_;
+  }
+
+  glia_stats stats() const override { return st_; }
+  void reset_stats() override { st_ = glia_stats{}; }
+
+ private:
+  // ------------------------------------------------------------------------------------------
+  // memory, transforms, transfers
+  // ------------------------------------------------------------------------------------------
+  template <typename T>
+  T* dalloc(int64_t count) {
+    void* p = nullptr;
+    const size_t b = (size_t)std::max<int64_t>(count, 1) * sizeof(T);
+    GLIA_CUDA(cudaMalloc(&p, b));
+    sizes_[p] = b;
+    bytes_ += (int64_t)b;
+    return (T*)p;
+  }
+  void dfree(void* p) {
+    auto it = sizes_.find(p);
+    if (it == sizes_.end()) return;
+    cudaStreamSynchronize(stream_);
+    bytes_ -= (int64_t)it->second;
+    sizes_.erase(it);
+    cudaFree(p);
+  }
+  R* fld() { return dalloc<R>(N_); }
+  R* spec() { return dalloc<R>(2 * Ns_); }
+  void fill(R* f, double v) {
+    k_fill<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, f, v);
+    GLIA_LAUNCH_CHECK();
+  }
+
+  cufftHandle make_plan(cufftType type, int batch, size_t* ws) {
+    cufftHandle p;
+    GLIA_CUFFT(cufftCreate(&p));
+    GLIA_CUFFT(cufftSetAutoAllocation(p, 0));
+    int dims[3] = {g_.n, g_.n, g_.n};
+    const bool fwd = (type == CUFFT_R2C || type == CUFFT_D2Z);
+    GLIA_CUFFT(cufftMakePlanMany(p, 3, dims, nullptr, 1, fwd ? (int)N_ : (int)Ns_, nullptr, 1,
+                                 fwd ? (int)Ns_ : (int)N_, type, batch, ws));
+    GLIA_CUFFT(cufftSetStream(p, stream_));
+    return p;
+  }
+  void make_plans() {
+    size_t w[4] = {0, 0, 0, 0};
+    r2c1_ = make_plan(CT<R>::kR2C, 1, &w[0]);
+    c2r1_ = make_plan(CT<R>::kC2R, 1, &w[1]);
+    r2c3_ = make_plan(CT<R>::kR2C, 3, &w[2]);
+    c2r3_ = make_plan(CT<R>::kC2R, 3, &w[3]);
+    fft_ws_bytes_ = std::max({w[0], w[1], w[2], w[3], (size_t)16});
+    fft_ws_ = dalloc<char>((int64_t)fft_ws_bytes_);
+    for (cufftHandle p : {r2c1_, c2r1_, r2c3_, c2r3_}) GLIA_CUFFT(cufftSetWorkArea(p, fft_ws_));
+  }
+  void ensure_batch_plans(int B) {
+    destroy_batch_plans();
+    size_t w[2] = {0, 0};
+    r2cB_ = make_plan(CT<R>::kR2C, B, &w[0]);
+    c2rB_ = make_plan(CT<R>::kC2R, B, &w[1]);
+    const size_t need = std::max(w[0], w[1]);
+    if (need > fft_ws_bytes_) {
+      batch_ws_ = dalloc<char>((int64_t)need);
+      GLIA_CUFFT(cufftSetWorkArea(r2cB_, batch_ws_));
+      GLIA_CUFFT(cufftSetWorkArea(c2rB_, batch_ws_));
+    } else {
+      GLIA_CUFFT(cufftSetWorkArea(r2cB_, fft_ws_));
+      GLIA_CUFFT(cufftSetWorkArea(c2rB_, fft_ws_));
+    }
+  }
+  void destroy_batch_plans() {
+    if (r2cB_) cufftDestroy(r2cB_);
+    if (c2rB_) cufftDestroy(c2rB_);
+    r2cB_ = c2rB_ = 0;
+    if (batch_ws_) {
+      dfree(batch_ws_);
+      batch_ws_ = nullptr;
+    }
+  }
+  void r2c(cufftHandle p, const R* in, R* out, int batch = 1) {
+    if constexpr (std::is_same<R, float>::value)
+      GLIA_CUFFT(cufftExecR2C(p, const_cast<float*>(in), reinterpret_cast<cufftComplex*>(out)));
+    else
+      GLIA_CUFFT(cufftExecD2Z(p, const_cast<double*>(in),
+                              reinterpret_cast<cufftDoubleComplex*>(out)));
+    st_.total_fft_execs += batch;
+  }
+  void c2r(cufftHandle p, R* in, R* out, int batch = 1) {
+    if constexpr (std::is_same<R, float>::value)
+      GLIA_CUFFT(cufftExecC2R(p, reinterpret_cast<cufftComplex*>(in), out));
+    else
+      GLIA_CUFFT(cufftExecZ2D(p, reinterpret_cast<cufftDoubleComplex*>(in), out));
+    st_.total_fft_execs += batch;
+  }
+
+  SolveStatus read_status() {
+    GLIA_CUDA(cudaMemcpyAsync(&hsc_->it, &sc_->it, 3 * sizeof(int), cudaMemcpyDeviceToHost,
+                              stream_));
+    GLIA_CUDA(cudaMemcpyAsync(&hsc_->dp, &sc_->dp, sizeof(double), cudaMemcpyDeviceToHost,
+                              stream_));
+    GLIA_CUDA(cudaStreamSynchronize(stream_));
+    return SolveStatus{hsc_->status, hsc_->it, hsc_->dp};
+  }
+  double read_red(int slot) {
+    GLIA_CUDA(cudaMemcpyAsync(&hsc_->red[slot], &sc_->red[slot], sizeof(double),
+                              cudaMemcpyDeviceToHost, stream_));
+    GLIA_CUDA(cudaStreamSynchronize(stream_));
+    return hsc_->red[slot];
+  }
+
+  double* stage() {
+    if (!stage_) stage_ = dalloc<double>(N_);
+    return stage_;
+  }
+  // grid field in the caller's pointer mode -> device field of type R
+  void import_field(const void* src, R* dst) {
+    if (!src) throw Error(GLIA_ERR_INVALID, "null field pointer");
+    const size_t nb = (size_t)N_;
+    if (ptr_mode_ == GLIA_PTR_HOST_F64) {
+      if constexpr (std::is_same<R, double>::value) {
+        GLIA_CUDA(cudaMemcpyAsync(dst, src, nb * 8, cudaMemcpyHostToDevice, stream_));
+      } else {
+        GLIA_CUDA(cudaMemcpyAsync(stage(), src, nb * 8, cudaMemcpyHostToDevice, stream_));
+        k_convert<double, R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, stage(), dst);
+        GLIA_LAUNCH_CHECK();
+      }
+    } else if (ptr_mode_ == GLIA_PTR_DEVICE_F64) {
+      if constexpr (std::is_same<R, double>::value) {
+        if (src != dst)
+          GLIA_CUDA(cudaMemcpyAsync(dst, src, nb * 8, cudaMemcpyDeviceToDevice, stream_));
+      } else {
+        k_convert<double, R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, (const double*)src, dst);
+        GLIA_LAUNCH_CHECK();
+      }
+    } else {
+      if constexpr (std::is_same<R, float>::value) {
+        if (src != dst)
+          GLIA_CUDA(cudaMemcpyAsync(dst, src, nb * 4, cudaMemcpyDeviceToDevice, stream_));
+      } else {
+        k_convert<float, R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, (const float*)src, dst);
+        GLIA_LAUNCH_CHECK();
+      }
+    }
+  }
+  void export_field(const R* src, void* dst) {
+    if (!dst) throw Error(GLIA_ERR_INVALID, "null field pointer");
+    const size_t nb = (size_t)N_;
+    if (ptr_mode_ == GLIA_PTR_HOST_F64) {
+      if constexpr (std::is_same<R, double>::value) {
+        GLIA_CUDA(cudaMemcpyAsync(dst, src, nb * 8, cudaMemcpyDeviceToHost, stream_));
+      } else {
+        k_convert<R, double><<<pw_blocks_, kThreads, 0, stream_>>>(N_, src, stage());
+        GLIA_LAUNCH_CHECK();
+        GLIA_CUDA(cudaMemcpyAsync(dst, stage(), nb * 8, cudaMemcpyDeviceToHost, stream_));
+      }
+      GLIA_CUDA(cudaStreamSynchronize(stream_));
+    } else if (ptr_mode_ == GLIA_PTR_DEVICE_F64) {
+      if constexpr (std::is_same<R, double>::value) {
+        if (src != dst)
+          GLIA_CUDA(cudaMemcpyAsync(dst, src, nb * 8, cudaMemcpyDeviceToDevice, stream_));
+      } else {
+        k_convert<R, double><<<pw_blocks_, kThreads, 0, stream_>>>(N_, src, (double*)dst);
+        GLIA_LAUNCH_CHECK();
+      }
+    } else {
+      if constexpr (std::is_same<R, float>::value) {
+        if (src != dst)
+          GLIA_CUDA(cudaMemcpyAsync(dst, src, nb * 4, cudaMemcpyDeviceToDevice, stream_));
+      } else {
+        k_convert<R, float><<<pw_blocks_, kThreads, 0, stream_>>>(N_, src, (float*)dst);
+        GLIA_LAUNCH_CHECK();
+      }
+    }
+  }
+
+  // ------------------------------------------------------------------------------------------
+  Geo g_;
+  bool ref_;
+  int sms_ = 0, red_blocks_ = 0, pw_blocks_ = 0;
+  int64_t N_ = 0, Ns_ = 0;
+  cudaStream_t stream_ = nullptr, own_stream_ = nullptr;
+  int ptr_mode_ = GLIA_PTR_HOST_F64;
+  std::unordered_map<void*, size_t> sizes_;
+  int64_t bytes_ = 0;
+
+  cufftHandle r2c1_ = 0, c2r1_ = 0, r2c3_ = 0, c2r3_ = 0, r2cB_ = 0, c2rB_ = 0;
+  char* fft_ws_ = nullptr;
+  char* batch_ws_ = nullptr;
+  size_t fft_ws_bytes_ = 0;
+
+  DevScalars* sc_ = nullptr;
+  DevScalars* hsc_ = nullptr;
+  SolveStatus* hst_ = nullptr;
+  RedWs ws_{};
+
+  // TumorParameters / solver settings
+  double dt_ = 0.5;
+  int nt_ = 1, order_ = 2;
+  bool adjoint_store_ = false;
+  int hist_mode_ = GLIA_HISTORY_FULL, every_ = 10;
+  double rtol_ = 1e-6, abstol_ = 1e-50, divtol_ = 1e4;
+  int maxit_ = 5000, pc_dt_mode_ = GLIA_PC_DT_REFERENCE;
+  double pc_dt_fixed_ = 0, ctx_dt_ = 0.5, pc_kbar_ = 0, pc_dt_ = 0.5;
+  int ksp_itr_ = 0;
+  glia_opt_settings opt_{1, 1, 1, 0, 1, 0, 1e-4, 1.0, 1.0, 0, 0};
+  glia_stats st_{};
+
+  // MatProp / DiffCoef / ReacCoef
+  R *wm_ = nullptr, *gm_ = nullptr, *csf_ = nullptr, *vt_ = nullptr, *bg_ = nullptr,
+    *filter_ = nullptr, *kxx_ = nullptr, *rho_ = nullptr, *obs_ = nullptr;
+  bool tissue_set_ = false, kxx_sinusoidal_ = false;
+  double filter_sum_ = 0, k_scale_ = 1e-2, kxx_avg_ = 0, k_gm_wm_ = 0, k_glm_wm_ = 0;
+  double rho_scale_ = 0, r_gm_wm_ = 0, r_glm_wm_ = 0;
+
+  // Tumor state and work
+  R *c0_ = nullptr, *ct_ = nullptr, *p0_ = nullptr, *pt_ = nullptr, *tmp_ = nullptr,
+    *tmp2_ = nullptr, *d1_ = nullptr;
+  R *chat_ = nullptr, *xhat_ = nullptr, *rhat_ = nullptr, *phat_ = nullptr, *what_ = nullptr;
+  R *g3s_ = nullptr, *g3r_ = nullptr, *ga3_ = nullptr;
+  R* wkern_ = nullptr;
+  double wkern_sigma_ = -1;
+  double* stage_ = nullptr;
+
+  // reference-structured path
+  R* t_[8] = {};
+  R *rb_ = nullptr, *rr_ = nullptr, *rz_ = nullptr, *rp_ = nullptr, *rw_ = nullptr,
+    *rt2_ = nullptr;
+  R *kxy_ = nullptr, *kxz_ = nullptr, *kyz_ = nullptr, *kyy_ = nullptr, *kzz_ = nullptr;
+  R *wh_ = nullptr, *pf_ = nullptr;
+
+  // history
+  std::vector<R*> c_hist_, c_half_, chat_hist_, p_hist_, ckpt_, seg_c_, seg_half_, seg_chat_;
+  bool state_done_ = false, adjoint_done_ = false, trick_at_state_ = false,
+       kappa_used_trick_ = false;
+
+  // Phi
+  int phi_np_ = 0, cells_per_dim_ = 0;
+  double phi_sigma_ = 0;
+  std::vector<double> centers_, phi_max_each_, hphi_p_;
+  std::vector<PhiBox> phi_box_h_;
+  R* phi_store_ = nullptr;
+  PhiBox* phi_boxes_ = nullptr;
+  double* phi_centers_ = nullptr;
+  double* phi_p_ = nullptr;
+  int *cell_ptr_ = nullptr, *cell_list_ = nullptr;
+};
+
+}  // namespace glia

@@ -1,0 +1,160 @@
+"""CUDA library against the FP64 CPU oracle on the same seeded inputs (GPU machine only).
+
+Every comparison goes through the C-ABI (include/glia_rd.h). Bars: FP64 state rel-L2 <= 1e-5,
+mixed (FP32 bulk, FP64 reductions) <= 1e-4, gradients <= 1e-4; PCG iteration counts equal for
+FP64.
+"""
+import numpy as np
+import pytest
+
+from glia_gb300 import _abi
+from tests.gpu_common import (FP64, FUSED, GRAD_TOL, MIXED, REFERENCE, STATE_TOL, configure,
+                              gpu, observation, orc, small_problem)
+from tests.helpers import reference_test_field, rel_l2
+from tests.test_oracle_pins import CATCH_EPS, run_pdesolver
+
+pytestmark = pytest.mark.gpu
+
+ENGINES = [(FP64, FUSED), (MIXED, FUSED), (FP64, REFERENCE)]
+
+
+@pytest.mark.parametrize("prec,eng", ENGINES + [(MIXED, REFERENCE)])
+def test_pdesolver_known_answer(prec, eng):
+    """src/test/pdesolver.cpp:46-48 through glia_diffusion_solve."""
+    c, its = run_pdesolver(gpu(64, prec, eng))
+    nrm = np.linalg.norm(c)
+    tol = CATCH_EPS * 2.0487 if prec == FP64 else 1e-4 * 2.0487
+    assert abs(nrm - 2.0487) <= tol, nrm
+    assert its == 5
+
+
+@pytest.mark.parametrize("prec,eng", ENGINES)
+def test_apply_d_and_smoother(prec, eng):
+    n = 32
+    wl, tissue, centers = small_problem(n)
+    o, g = orc(n), gpu(n, prec, eng)
+    for ctx in (o, g):
+        configure(ctx, wl, tissue, centers)
+    f = reference_test_field(n) + 0.1 * tissue.wm.reshape(-1)
+    tol = 1e-11 if prec == FP64 else 2e-5
+    assert rel_l2(g.apply_d(f), o.apply_d(f)) < tol
+    s = 2 * np.pi / n
+    assert rel_l2(g.smooth(f, s), o.smooth(f, s)) < tol
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+@pytest.mark.parametrize("phi_store", [0, 1])
+def test_phi_apply_and_transpose(prec, phi_store):
+    n = 32
+    wl, tissue, centers = small_problem(n, n_gauss=8)
+    o, g = orc(n), gpu(n, prec)
+    for ctx in (o, g):
+        configure(ctx, wl, tissue, centers)
+        ctx.set_opt(phi_store=phi_store)
+    p = np.linspace(0.0, 1.0, len(centers))
+    p[1] = 0.0
+    tol = 1e-12 if prec == FP64 else 2e-6
+    assert rel_l2(g.phi_apply(p), o.phi_apply(p)) < tol
+    v = reference_test_field(n) + tissue.gm.reshape(-1)
+    assert rel_l2(g.phi_apply_transpose(v, len(p)), o.phi_apply_transpose(v, len(p))) < tol
+
+
+@pytest.mark.parametrize("prec,eng", ENGINES)
+def test_solve_state_and_adjoint(prec, eng):
+    n, nt = 32, 6
+    wl, tissue, centers = small_problem(n, nt)
+    o, g = orc(n), gpu(n, prec, eng)
+    for ctx in (o, g):
+        configure(ctx, wl, tissue, centers)
+        ctx.set_history(_abi.GLIA_HISTORY_FULL, 0, 0)
+    p = np.zeros(len(centers))
+    p[:3] = [1.0, 0.5, 0.25]
+    c0 = o.phi_apply(p)
+    c1o, c1g = o.solve_state(c0), g.solve_state(c0)
+    assert rel_l2(c1g, c1o) < STATE_TOL[prec]
+    so, sg = o.stats(), g.stats()
+    if prec == FP64:
+        assert sg["diff_ksp_itr_state"] == so["diff_ksp_itr_state"]
+    for i in (1, nt // 2):
+        assert rel_l2(g.get_state(i), o.get_state(i)) < STATE_TOL[prec]
+    pt = -(c1o - 0.5 * c1o.max())
+    a0o, a0g = o.solve_adjoint(pt), g.solve_adjoint(pt)
+    assert rel_l2(a0g, a0o) < STATE_TOL[prec]
+
+
+@pytest.mark.parametrize("prec,eng", ENGINES)
+def test_objective_and_gradient(prec, eng):
+    n, nt = 32, 6
+    wl, tissue, centers = small_problem(n, nt)
+    d1 = observation(wl, tissue, centers)
+    o, g = orc(n), gpu(n, prec, eng)
+    for ctx in (o, g):
+        configure(ctx, wl, tissue, centers)
+        ctx.set_obs_filter(np.ones(n ** 3))
+    x = np.concatenate([np.linspace(0.1, 0.9, len(centers)), [wl.kappa, wl.rho]])
+    Jo, gro = o.eval_objective_and_gradient(x, d1)
+    Jg, grg = g.eval_objective_and_gradient(x, d1)
+    assert abs(Jg - Jo) <= 1e-6 * abs(Jo) if prec == FP64 else abs(Jg - Jo) <= 1e-4 * abs(Jo)
+    assert rel_l2(grg, gro) < GRAD_TOL
+    # each block of the gradient on its own
+    np_ = len(centers)
+    assert rel_l2(grg[:np_], gro[:np_]) < GRAD_TOL
+    assert abs(grg[np_] - gro[np_]) <= GRAD_TOL * abs(gro[np_])
+    assert abs(grg[np_ + 1] - gro[np_ + 1]) <= GRAD_TOL * abs(gro[np_ + 1])
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+def test_checkpointed_gradient_equals_full_history(prec):
+    n, nt = 32, 10
+    wl, tissue, centers = small_problem(n, nt)
+    d1 = observation(wl, tissue, centers)
+    x = np.concatenate([np.linspace(0.1, 0.9, len(centers)), [wl.kappa, wl.rho]])
+    out = []
+    for hist, every in ((_abi.GLIA_HISTORY_FULL, 0), (_abi.GLIA_HISTORY_CHECKPOINT, 3),
+                        (_abi.GLIA_HISTORY_CHECKPOINT, 10)):
+        g = gpu(n, prec)
+        configure(g, wl, tissue, centers, hist, every)
+        g.set_obs_filter(np.ones(n ** 3))
+        out.append(g.eval_objective_and_gradient(x, d1))
+    for J, gr in out[1:]:
+        assert J == out[0][0]
+        assert rel_l2(gr, out[0][1]) < 1e-12
+
+
+def test_grad_objective_known_answer_gpu():
+    """src/test/grad.cpp:7-80 on the CUDA library (FP64, 64^3, nt = 100)."""
+    n = 64
+    g = gpu(n, FP64)
+    g.set_time(0.01, 100, 2)
+    g.set_tissue_sinusoidal()
+    g.set_coefficients(k=0.01, rho=10.0)
+    g.set_opt(np=1, nk=1, nr=1, flag_reaction_inv=1, diffusivity_inversion=1, beta=0.0)
+    x = np.array([0.0, 0.01, 0.01])
+    zeros = np.zeros(n ** 3)
+    g.set_c0(reference_test_field(n))
+    g.eval_objective(x, zeros)
+    data = g.get_state(100)
+    assert g.eval_objective(x, data) < 1e-7
+    assert g.eval_objective(x, zeros) > 0
+
+
+def test_gradient_matches_central_differences():
+    """Adjoint p-gradient vs central finite differences (h = 1e-3) on random directions."""
+    n, nt = 32, 6
+    wl, tissue, centers = small_problem(n, nt)
+    d1 = observation(wl, tissue, centers)
+    g = gpu(n, FP64)
+    configure(g, wl, tissue, centers)
+    g.set_obs_filter(np.ones(n ** 3))
+    g.set_opt(all_gradients=0, diffusivity_inversion=0)  # p only: the exact discrete adjoint
+    g.set_pcg(1e-11, 5000)  # converged solves, so J is smooth in x
+    x = np.concatenate([np.linspace(0.1, 0.9, len(centers)), [wl.kappa, wl.rho]])
+    _, gr = g.eval_objective_and_gradient(x, d1)
+    rng = np.random.default_rng(3)
+    for _ in range(3):
+        d = np.zeros_like(x)
+        d[: len(centers)] = rng.standard_normal(len(centers))
+        d /= np.linalg.norm(d)
+        h = 1e-3
+        fd = (g.eval_objective(x + h * d, d1) - g.eval_objective(x - h * d, d1)) / (2 * h)
+        assert abs(fd - gr @ d) <= 1e-4 * max(abs(fd), 1e-12), (fd, gr @ d)
