@@ -122,6 +122,9 @@ SIGNATURES = {
     "eval_objective_and_gradient": (c_int, [_CTX, _D, c_int, _P, _D, _D]),
     "get_stats": (c_int, [_CTX, POINTER(GliaStats)]),
     "reset_stats": (c_int, [_CTX]),
+    "set_timing": (c_int, [_CTX, c_int]),
+    "get_timing": (c_int, [_CTX, c_int, POINTER(c_char_p), POINTER(c_int64), POINTER(c_double),
+                           POINTER(c_double)]),
 }
 
 

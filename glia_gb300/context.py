@@ -304,6 +304,25 @@ class Context:
     def reset_stats(self):
         self._call("reset_stats", self.api.reset_stats)
 
+    def set_timing(self, enable: bool):
+        self._call("set_timing", self.api.set_timing, int(enable))
+
+    def timing(self) -> dict:
+        """Per-kernel {name: (launches, ms, algorithmic_bytes)} since timing was enabled."""
+        out = {}
+        slot, count = 0, 1
+        while slot < count:
+            name = ctypes.c_char_p()
+            launches, ms, b = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double()
+            rc = self.api.get_timing(self._h, slot, ctypes.byref(name), ctypes.byref(launches),
+                                     ctypes.byref(ms), ctypes.byref(b))
+            if rc < 0:
+                self._check(rc, "get_timing")
+            count = rc
+            out[name.value.decode()] = (launches.value, ms.value, b.value)
+            slot += 1
+        return out
+
     def synchronize(self):
         self._call("synchronize", self.api.synchronize)
 

@@ -255,5 +255,16 @@ int glia_get_stats(const glia_ctx* ctx, glia_stats* st) {
 int glia_reset_stats(glia_ctx* ctx) {
   return guarded(ctx, [&](glia::EngineBase& e) { e.reset_stats(); });
 }
+int glia_set_timing(glia_ctx* ctx, int enable) {
+  return guarded(ctx, [&](glia::EngineBase& e) { e.set_timing(enable != 0); });
+}
+int glia_get_timing(glia_ctx* ctx, int slot, const char** name, int64_t* launches, double* ms,
+                    double* algorithmic_bytes) {
+  int count = 0;
+  int rc = guarded(ctx, [&](glia::EngineBase& e) {
+    count = e.timing(slot, name, launches, ms, algorithmic_bytes);
+  });
+  return rc == GLIA_OK ? count : rc;
+}
 
 }  // extern "C"

@@ -41,6 +41,9 @@ class EngineBase {
   virtual void evaluate(const double* x, int nx, const void* d1, double* J, double* dJ) = 0;
   virtual glia_stats stats() const = 0;
   virtual void reset_stats() = 0;
+  virtual void set_timing(bool on) = 0;
+  virtual int timing(int slot, const char** name, int64_t* launches, double* ms,
+                     double* bytes) = 0;
 };
 
 EngineBase* make_engine_f32(int n, bool reference_structured);

@@ -21,6 +21,15 @@
 
 #include "engine.hpp"
 #include "kernels.cuh"
+#include "ktimer.cuh"
+
+#define GLIA_TIMED(slot, bytes, ...)             \
+  do {                                           \
+    cudaEvent_t ev_ = tm_.begin(stream_);        \
+    __VA_ARGS__;                                 \
+    GLIA_LAUNCH_CHECK();                         \
+    tm_.end((slot), ev_, (double)(bytes), stream_); \
+  } while (0)
 
 namespace glia {
 
@@ -275,19 +284,19 @@ class Engine final : public EngineBase {
     r2c(r2c1_, c, chat);
     launch_grad3<false>(chat, nullptr);
     apply_k_spectral();
-    k_spec_div<R, EPI_SETUP><<<red_blocks_, kThreads, 0, stream_>>>(g_, g3s_, chat, cx, xhat_,
-                                                                     rhat_, R(0), sc_, ws_);
-    GLIA_LAUNCH_CHECK();
+    GLIA_TIMED(KS_DIV_SETUP, SB() * (cx ? 7 : 6),
+               k_spec_div<R, EPI_SETUP><<<red_blocks_, kThreads, 0, stream_>>>(
+                   g_, g3s_, chat, cx, xhat_, rhat_, R(0), sc_, ws_));
     SolveStatus s = read_status();
     while (s.status == 0) {
       launch_grad3<true>(rhat_, phat_);  // p = P r + b p, gradient spectra of p
       apply_k_spectral();                // 3 C2R, k *, 3 R2C
-      k_spec_div<R, EPI_CGW><<<red_blocks_, kThreads, 0, stream_>>>(g_, g3s_, phat_, nullptr,
-                                                                     what_, nullptr, R(0), sc_, ws_);
-      GLIA_LAUNCH_CHECK();
-      k_cg_update<R><<<red_blocks_, kThreads, 0, stream_>>>(g_, xhat_, phat_, rhat_, what_, sc_,
-                                                            ws_);
-      GLIA_LAUNCH_CHECK();
+      GLIA_TIMED(KS_DIV_CGW, SB() * 5,
+                 k_spec_div<R, EPI_CGW><<<red_blocks_, kThreads, 0, stream_>>>(
+                     g_, g3s_, phat_, nullptr, what_, nullptr, R(0), sc_, ws_));
+      GLIA_TIMED(KS_CG_UPDATE, SB() * 6,
+                 k_cg_update<R><<<red_blocks_, kThreads, 0, stream_>>>(g_, xhat_, phat_, rhat_,
+                                                                       what_, sc_, ws_));
       s = read_status();
     }
     c2r(c2r1_, xhat_, c);  // x = F^-1 (x')
@@ -296,14 +305,15 @@ class Engine final : public EngineBase {
 
   template <bool CGDIR>
   void launch_grad3(const R* src, R* pdir) {
-    k_spec_grad3<R, CGDIR><<<pw_blocks_, kThreads, 0, stream_>>>(g_, src, pdir, g3s_, sc_);
-    GLIA_LAUNCH_CHECK();
+    GLIA_TIMED(CGDIR ? KS_SPEC_GRAD3_CG : KS_SPEC_GRAD3, SB() * (CGDIR ? 6 : 4),
+               k_spec_grad3<R, CGDIR><<<pw_blocks_, kThreads, 0, stream_>>>(g_, src, pdir, g3s_,
+                                                                            sc_));
   }
   // gradient spectra (g3s_) -> real gradient -> times k -> spectra of k * grad (g3s_)
   void apply_k_spectral() {
     c2r(c2r3_, g3s_, g3r_, 3);
-    k_mul_k3<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, g3r_, kxx_, sc_, 0);
-    GLIA_LAUNCH_CHECK();
+    GLIA_TIMED(KS_MUL_K3, FB() * 7,
+               k_mul_k3<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, g3r_, kxx_, sc_, 0));
     r2c(r2c3_, g3r_, g3s_, 3);
   }
 
@@ -330,24 +340,23 @@ class Engine final : public EngineBase {
     for (R* f : {kxy_, kxz_, kyz_}) GLIA_CUDA(cudaMemsetAsync(f, 0, N_ * sizeof(R), stream_));
   }
   void vaxpy(R* y, double a, const R* x) {
-    k_axpy<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, y, a, x);
-    GLIA_LAUNCH_CHECK();
+    GLIA_TIMED(KS_REF_VEC, FB() * 3, k_axpy<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, y, a, x));
   }
   void vaypx(R* y, double b, const R* x) {
-    k_aypx<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, y, b, x);
-    GLIA_LAUNCH_CHECK();
+    GLIA_TIMED(KS_REF_VEC, FB() * 3, k_aypx<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, y, b, x));
   }
   void vmult(R* z, const R* x, const R* y) {
-    k_pointwise_mult<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, z, x, y);
-    GLIA_LAUNCH_CHECK();
+    GLIA_TIMED(KS_REF_VEC, FB() * 3,
+               k_pointwise_mult<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, z, x, y));
   }
   void vcopy(R* y, const R* x) {
-    GLIA_CUDA(cudaMemcpyAsync(y, x, N_ * sizeof(R), cudaMemcpyDeviceToDevice, stream_));
+    GLIA_TIMED(KS_COPY, FB() * 2,
+               GLIA_CUDA(cudaMemcpyAsync(y, x, N_ * sizeof(R), cudaMemcpyDeviceToDevice, stream_)));
   }
   void vzero(R* y) { GLIA_CUDA(cudaMemsetAsync(y, 0, N_ * sizeof(R), stream_)); }
   double vdot(const R* x, const R* y) {  // PETSc VecDot: one reduction, scalar to the host
-    k_dot<R><<<red_blocks_, kThreads, 0, stream_>>>(N_, x, y, sc_, 0, ws_);
-    GLIA_LAUNCH_CHECK();
+    GLIA_TIMED(KS_REF_DOT, FB() * 2,
+               k_dot<R><<<red_blocks_, kThreads, 0, stream_>>>(N_, x, y, sc_, 0, ws_));
     return read_red(0);
   }
   // SpectralOperators::computeGradient (src/grad/SpectralOperators.cpp:100-177)
@@ -355,8 +364,8 @@ class Engine final : public EngineBase {
     r2c(r2c1_, x, xhat_);
     R* out[3] = {gx, gy, gz};
     for (int d = 0; d < 3; d++) {
-      k_mult_wavenumber<R><<<pw_blocks_, kThreads, 0, stream_>>>(g_, d, xhat_, wh_);
-      GLIA_LAUNCH_CHECK();
+      GLIA_TIMED(KS_REF_VEC, SB() * 2,
+                 k_mult_wavenumber<R><<<pw_blocks_, kThreads, 0, stream_>>>(g_, d, xhat_, wh_));
       c2r(c2r1_, wh_, out[d]);
     }
   }
@@ -366,8 +375,9 @@ class Engine final : public EngineBase {
     const int dim[3] = {0, 2, 1};
     for (int q = 0; q < 3; q++) {
       r2c(r2c1_, in[q], xhat_);
-      k_mult_wavenumber<R><<<pw_blocks_, kThreads, 0, stream_>>>(g_, dim[q], xhat_, wh_);
-      GLIA_LAUNCH_CHECK();
+      GLIA_TIMED(KS_REF_VEC, SB() * 2,
+                 k_mult_wavenumber<R><<<pw_blocks_, kThreads, 0, stream_>>>(g_, dim[q], xhat_,
+                                                                             wh_));
       c2r(c2r1_, wh_, q == 0 ? div : t_[7]);
       if (q) vaxpy(div, 1.0, t_[7]);
     }
@@ -392,8 +402,8 @@ class Engine final : public EngineBase {
   void ref_applyPC(R* y, const R* x) {  // applyPC (:182-215)
     vcopy(y, x);
     r2c(r2c1_, y, xhat_);
-    k_hadamard_real<R><<<pw_blocks_, kThreads, 0, stream_>>>(Ns_, xhat_, pf_);
-    GLIA_LAUNCH_CHECK();
+    GLIA_TIMED(KS_REF_VEC, SB() * 2 + Ns_ * sizeof(R),
+               k_hadamard_real<R><<<pw_blocks_, kThreads, 0, stream_>>>(Ns_, xhat_, pf_));
     c2r(c2r1_, xhat_, y);
   }
   // KSPSolve_CG + KSPConvergedDefault with host scalars, as PETSc runs them
@@ -538,6 +548,7 @@ class Engine final : public EngineBase {
     if (phi_boxes_) dfree(phi_boxes_);
     if (phi_centers_) dfree(phi_centers_);
     phi_store_ = dalloc<R>(std::max<int64_t>(off, 1));
+    phi_store_bytes_ = (double)off * sizeof(R);
     phi_boxes_ = dalloc<PhiBox>(np);
     phi_centers_ = dalloc<double>(3 * np);
     GLIA_CUDA(cudaMemcpyAsync(phi_boxes_, boxes.data(), np * sizeof(PhiBox),
@@ -642,15 +653,17 @@ class Engine final : public EngineBase {
     GLIA_CUDA(cudaMemcpyAsync(phi_p_, hphi_p_.data(), phi_np_ * sizeof(double),
                               cudaMemcpyHostToDevice, stream_));
     const int cells = cells_per_dim_ * cells_per_dim_ * cells_per_dim_;
-    k_phi_apply<R><<<cells, 512, 0, stream_>>>(g_, cells_per_dim_, cell_ptr_, cell_list_,
-                                                phi_boxes_, phi_store_, phi_p_, scale, out);
-    GLIA_LAUNCH_CHECK();
+    GLIA_TIMED(KS_PHI, FB() + phi_store_bytes_,
+               k_phi_apply<R><<<cells, 512, 0, stream_>>>(g_, cells_per_dim_, cell_ptr_,
+                                                           cell_list_, phi_boxes_, phi_store_,
+                                                           phi_p_, scale, out));
     GLIA_CUDA(cudaStreamSynchronize(stream_));  // hphi_p_ may be reused by the next call
   }
   void phi_applyT_from(const R* v, double* pout) {
     if (phi_np_ < 1) throw Error(GLIA_ERR_STATE, "Phi is not set (glia_set_phi)");
-    k_phi_applyT<R><<<phi_np_, kThreads, 0, stream_>>>(g_, phi_boxes_, phi_store_, v, phi_p_);
-    GLIA_LAUNCH_CHECK();
+    GLIA_TIMED(KS_PHI, 2.0 * phi_store_bytes_,
+               k_phi_applyT<R><<<phi_np_, kThreads, 0, stream_>>>(g_, phi_boxes_, phi_store_, v,
+                                                                   phi_p_));
     GLIA_CUDA(cudaMemcpyAsync(pout, phi_p_, phi_np_ * sizeof(double), cudaMemcpyDeviceToHost,
                               stream_));
     GLIA_CUDA(cudaStreamSynchronize(stream_));
@@ -748,8 +761,9 @@ class Engine final : public EngineBase {
     }
   }
   void reaction(R* c, R* half_out) {
-    k_reaction_fwd<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, c, rho_, (R)dt_, half_out);
-    GLIA_LAUNCH_CHECK();
+    GLIA_TIMED(KS_REACTION, FB() * (half_out ? 4 : 3),
+               k_reaction_fwd<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, c, rho_, (R)dt_,
+                                                                        half_out));
   }
 
   // PdeOperatorsRD::solveState(0) (src/pde/PdeOperators.cpp:235-316)
@@ -801,8 +815,9 @@ class Engine final : public EngineBase {
     }
   }
   void reaction_adjoint(const R* chalf) {
-    k_reaction_lin<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, p0_, rho_, chalf, (R)dt_);
-    GLIA_LAUNCH_CHECK();
+    GLIA_TIMED(KS_REACTION_LIN, FB() * 4,
+               k_reaction_lin<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, p0_, rho_, chalf,
+                                                                        (R)dt_));
   }
   // reactionAdjoint without stored half steps (src/pde/PdeOperators.cpp:331-344)
   const R* recompute_half(const R* ci) {
@@ -814,9 +829,9 @@ class Engine final : public EngineBase {
   // per-time-point gradient terms at time point i (state c_i, adjoint alpha_i in p0_)
   void grad_point(int i, const R* ci, bool explicit_kappa) {
     const double w = (i == 0 || i == nt_) ? 0.5 : 1.0;
-    k_grad_rho_acc<R><<<red_blocks_, kThreads, 0, stream_>>>(N_, ci, p0_, wm_, gm_, csf_, w * dt_,
-                                                              sc_, ws_);
-    GLIA_LAUNCH_CHECK();
+    GLIA_TIMED(KS_GRAD_ACC, FB() * 5,
+               k_grad_rho_acc<R><<<red_blocks_, kThreads, 0, stream_>>>(
+                   N_, ci, p0_, wm_, gm_, csf_, w * dt_, sc_, ws_));
     if (explicit_kappa) {
       R* gc = g3r_;
       R* ga = ga3();
@@ -827,9 +842,9 @@ class Engine final : public EngineBase {
         grad_real(ci, gc);
         grad_real(p0_, ga);
       }
-      k_grad_kappa_acc<R><<<red_blocks_, kThreads, 0, stream_>>>(N_, gc, ga, wm_, gm_, csf_,
-                                                                  w * dt_, sc_, ws_);
-      GLIA_LAUNCH_CHECK();
+      GLIA_TIMED(KS_GRAD_ACC, FB() * 9,
+                 k_grad_kappa_acc<R><<<red_blocks_, kThreads, 0, stream_>>>(
+                     N_, gc, ga, wm_, gm_, csf_, w * dt_, sc_, ws_));
     }
   }
   R* ga3() {
@@ -980,9 +995,9 @@ class Engine final : public EngineBase {
     if (apply_phi()) phi_apply_into(c0_, x);
     solve_state_internal();
     const double h = 2.0 * M_PI / g_.n, h3 = h * h * h;
-    k_obs_residual<R><<<red_blocks_, kThreads, 0, stream_>>>(N_, ct_, obs_, data,
-                                                             want_grad ? pt_ : nullptr, sc_, ws_);
-    GLIA_LAUNCH_CHECK();
+    GLIA_TIMED(KS_OBS, FB() * (want_grad ? 4 : 3),
+               k_obs_residual<R><<<red_blocks_, kThreads, 0, stream_>>>(
+                   N_, ct_, obs_, data, want_grad ? pt_ : nullptr, sc_, ws_));
     const double m1 = read_red(0);
     if (want_grad) {
       solve_adjoint_internal(true);
@@ -1076,6 +1091,22 @@ class Engine final : public EngineBase {
   }
 
   glia_stats stats() const override { return st_; }
+  void set_timing(bool on) override {
+    GLIA_CUDA(cudaStreamSynchronize(stream_));
+    tm_.harvest();
+    tm_.reset();
+    tm_.on = on;
+  }
+  int timing(int slot, const char** name, int64_t* launches, double* ms, double* bytes) override {
+    if (slot < 0 || slot >= KS_COUNT) throw Error(GLIA_ERR_INVALID, "timing: slot out of range");
+    GLIA_CUDA(cudaStreamSynchronize(stream_));
+    tm_.harvest();
+    if (name) *name = kSlotNames[slot];
+    if (launches) *launches = tm_.slots[slot].launches;
+    if (ms) *ms = tm_.slots[slot].ms;
+    if (bytes) *bytes = tm_.slots[slot].bytes;
+    return KS_COUNT;
+  }
   void reset_stats() override { st_ = glia_stats{}; }
 
  private:
@@ -1100,6 +1131,8 @@ class Engine final : public EngineBase {
     cudaFree(p);
   }
   R* fld() { return dalloc<R>(N_); }
+  double FB() const { return (double)N_ * sizeof(R); }         // bytes of one grid field
+  double SB() const { return 2.0 * (double)Ns_ * sizeof(R); }  // bytes of one half spectrum
   R* spec() { return dalloc<R>(2 * Ns_); }
   void fill(R* f, double v) {
     k_fill<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, f, v);
@@ -1151,7 +1184,21 @@ class Engine final : public EngineBase {
       batch_ws_ = nullptr;
     }
   }
+  int fft_slot(cufftHandle p, bool fwd) const {
+    if (p == r2c3_ || p == c2r3_) return fwd ? KS_FFT_R2C3 : KS_FFT_C2R3;
+    return fwd ? KS_FFT_R2C : KS_FFT_C2R;
+  }
   void r2c(cufftHandle p, const R* in, R* out, int batch = 1) {
+    cudaEvent_t ev = tm_.begin(stream_);
+    r2c_raw(p, in, out, batch);
+    tm_.end(fft_slot(p, true), ev, (double)batch * (FB() + SB()), stream_);
+  }
+  void c2r(cufftHandle p, R* in, R* out, int batch = 1) {
+    cudaEvent_t ev = tm_.begin(stream_);
+    c2r_raw(p, in, out, batch);
+    tm_.end(fft_slot(p, false), ev, (double)batch * (FB() + SB()), stream_);
+  }
+  void r2c_raw(cufftHandle p, const R* in, R* out, int batch) {
     if constexpr (std::is_same<R, float>::value)
       GLIA_CUFFT(cufftExecR2C(p, const_cast<float*>(in), reinterpret_cast<cufftComplex*>(out)));
     else
@@ -1159,7 +1206,7 @@ class Engine final : public EngineBase {
                               reinterpret_cast<cufftDoubleComplex*>(out)));
     st_.total_fft_execs += batch;
   }
-  void c2r(cufftHandle p, R* in, R* out, int batch = 1) {
+  void c2r_raw(cufftHandle p, R* in, R* out, int batch) {
     if constexpr (std::is_same<R, float>::value)
       GLIA_CUFFT(cufftExecC2R(p, reinterpret_cast<cufftComplex*>(in), out));
     else
@@ -1173,12 +1220,14 @@ class Engine final : public EngineBase {
     GLIA_CUDA(cudaMemcpyAsync(&hsc_->dp, &sc_->dp, sizeof(double), cudaMemcpyDeviceToHost,
                               stream_));
     GLIA_CUDA(cudaStreamSynchronize(stream_));
+    tm_.harvest();
     return SolveStatus{hsc_->status, hsc_->it, hsc_->dp};
   }
   double read_red(int slot) {
     GLIA_CUDA(cudaMemcpyAsync(&hsc_->red[slot], &sc_->red[slot], sizeof(double),
                               cudaMemcpyDeviceToHost, stream_));
     GLIA_CUDA(cudaStreamSynchronize(stream_));
+    tm_.harvest();
     return hsc_->red[slot];
   }
 
@@ -1256,6 +1305,7 @@ class Engine final : public EngineBase {
   int ptr_mode_ = GLIA_PTR_HOST_F64;
   std::unordered_map<void*, size_t> sizes_;
   int64_t bytes_ = 0;
+  KTimer tm_;
 
   cufftHandle r2c1_ = 0, c2r1_ = 0, r2c3_ = 0, c2r3_ = 0, r2cB_ = 0, c2rB_ = 0;
   char* fft_ws_ = nullptr;
@@ -1313,6 +1363,7 @@ class Engine final : public EngineBase {
   std::vector<double> centers_, phi_max_each_, hphi_p_;
   std::vector<PhiBox> phi_box_h_;
   R* phi_store_ = nullptr;
+  double phi_store_bytes_ = 0;
   PhiBox* phi_boxes_ = nullptr;
   double* phi_centers_ = nullptr;
   double* phi_p_ = nullptr;

@@ -39,7 +39,7 @@ def weierstrass_kernel(n: int, sigma: float) -> np.ndarray:
 def smooth(field: np.ndarray, sigma: float) -> np.ndarray:
     n = field.shape[0]
     k = weierstrass_kernel(n, sigma)
-    return np.fft.irfftn(np.fft.rfftn(k) * np.fft.rfftn(field), s=field.shape)
+    return np.fft.irfftn(np.fft.rfftn(k) * np.fft.rfftn(field), s=field.shape, axes=(0, 1, 2))
 
 
 @dataclass

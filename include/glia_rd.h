@@ -190,6 +190,15 @@ int glia_eval_objective_and_gradient(glia_ctx* ctx, const double* x, int nx, con
 int glia_get_stats(const glia_ctx* ctx, glia_stats* st);
 int glia_reset_stats(glia_ctx* ctx);
 
+/* ---- kernel timing (extension; no counterpart in the reference) ----------------------------
+ * While enabled, every launch of this library (kernels, cuFFT executions, copies) is bracketed
+ * by CUDA events on the context's stream and accumulated per kernel slot together with the
+ * algorithmic bytes the launch must move. Enabling clears the counters. glia_get_timing returns
+ * the number of slots (>= 1) or a negative status; slot names are static strings. */
+int glia_set_timing(glia_ctx* ctx, int enable);
+int glia_get_timing(glia_ctx* ctx, int slot, const char** name, int64_t* launches, double* ms,
+                    double* algorithmic_bytes);
+
 #ifdef __cplusplus
 }
 #endif
