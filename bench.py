@@ -399,8 +399,16 @@ def run_ours(args, torch, api, wl, tissue, centers, stream, ws, rank):
                     del_ctx.close()
                 torch.cuda.empty_cache()
         if ref_grad is not None:
+            npp = wl.n_gauss
             out["grad_rel_err_vs_fp64"] = float(np.linalg.norm(grad - ref_grad) /
                                                 np.linalg.norm(ref_grad))
+            out["grad_rel_err_blocks"] = {
+                "p": float(np.linalg.norm(grad[:npp] - ref_grad[:npp]) /
+                           np.linalg.norm(ref_grad[:npp])),
+                "kappa": float(abs(grad[npp] - ref_grad[npp]) / abs(ref_grad[npp])),
+                "rho": float(abs(grad[npp + 1] - ref_grad[npp + 1]) / abs(ref_grad[npp + 1]))}
+            out["grad_fp64"] = {"kappa": float(ref_grad[npp]), "rho": float(ref_grad[npp + 1]),
+                                "p_norm": float(np.linalg.norm(ref_grad[:npp]))}
         out["fp64_gpu"] = legs
         plain = legs.get("fp64_plain_reference_structured", {}).get("value")
         if plain:

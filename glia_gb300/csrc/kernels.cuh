@@ -40,9 +40,12 @@ __device__ __forceinline__ int conv_test(double rn, const DevScalars* s) {
   return 0;
 }
 
-__device__ __forceinline__ double pc_mult(double pcc, int wx, int wy, int wz) {
-  double v = 1.0 + pcc * (double)(wx * wx + wy * wy + wz * wz);
-  return v == 0.0 ? 1.0 : 1.0 / v;
+// spectral preconditioner multiplier 1 / (1 + pcc |w|^2) (precFactorDiffusion,
+// src/cuda/DiffCoef.cu:11-64, without the 1/N^3 factor, which the spectral-space PCG absorbs)
+template <typename R>
+__device__ __forceinline__ R pc_mult(R pcc, int wx, int wy, int wz) {
+  const R v = (R)1 + pcc * (R)(wx * wx + wy * wy + wz * wz);
+  return v == (R)0 ? (R)1 : (R)1 / v;
 }
 
 #define GRID_STRIDE(t, total)                                                    \
@@ -68,7 +71,7 @@ __global__ void __launch_bounds__(kThreads)
   const R invN = (R)g.invN;
   const bool first = CGDIR ? (sc->iter == 0) : true;
   const R b = CGDIR ? (R)sc->bcoef : R(0);
-  const double pcc = CGDIR ? sc->pc_c : 0.0;
+  const R pcc = CGDIR ? (R)sc->pc_c : R(0);
   GRID_STRIDE(t, nvec) {
     R v[K], pv[K], o0[K], o1[K], o2[K];
     V::ld(src + t * K, v);
@@ -78,7 +81,7 @@ __global__ void __launch_bounds__(kThreads)
       SpecIdx s = spec_index((uint32_t)(t * CPV + j), g);
       R re = v[2 * j], im = v[2 * j + 1];
       if (CGDIR) {
-        R P = (R)pc_mult(pcc, s.wx, s.wy, s.wz);
+        const R P = pc_mult<R>(pcc, s.wx, s.wy, s.wz);
         re *= P;
         im *= P;
         if (!first) {
@@ -147,9 +150,9 @@ __global__ void __launch_bounds__(kThreads)
   const int64_t nvec = g.Ns * 2 / K;
   const int64_t ss = g.Ns * 2;
   const R a = (R)(EPI == EPI_APPLYD ? 0.0 : sc->a_cn);
-  const double pcc = sc->pc_c;
+  const R pcc = (R)sc->pc_c;
   const R invN = (R)g.invN;
-  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  Acc<R> acc[4];
   GRID_STRIDE(t, nvec) {
     R g0[K], g1[K], g2[K], o[K], ax[K], cv[K];
     V::ld(G3 + t * K, g0);
@@ -169,13 +172,14 @@ __global__ void __launch_bounds__(kThreads)
         o[2 * j + 1] = di * scale;
       } else if (EPI == EPI_SETUP) {
         const R cr = ax[2 * j], ci = ax[2 * j + 1];
-        const double br = (double)cr + (double)a * dr, bi = (double)ci + (double)a * di;
+        const R br = cr + a * dr, bi = ci + a * di;
         const R rr = (R)2 * a * dr, ri = (R)2 * a * di;
-        const double P = pc_mult(pcc, s.wx, s.wy, s.wz);
-        acc[0] += s.mult * P * P * (br * br + bi * bi);
-        acc[1] += s.mult * P * P * ((double)rr * rr + (double)ri * ri);
-        acc[2] += s.mult * P * ((double)rr * rr + (double)ri * ri);
-        if (cx) acc[3] += s.mult * ((double)cv[2 * j] * dr + (double)cv[2 * j + 1] * di);
+        const R P = pc_mult<R>(pcc, s.wx, s.wy, s.wz), m = (R)s.mult;
+        const R r2 = rr * rr + ri * ri;
+        acc[0].add(m * P * P * (br * br + bi * bi));
+        acc[1].add(m * P * P * r2);
+        acc[2].add(m * P * r2);
+        if (cx) acc[3].add(m * (cv[2 * j] * dr + cv[2 * j + 1] * di));
         o[2 * j] = cr * invN;
         o[2 * j + 1] = ci * invN;
         ax[2 * j] = rr;
@@ -183,7 +187,7 @@ __global__ void __launch_bounds__(kThreads)
       } else {  // EPI_CGW
         const R pr = ax[2 * j], pi = ax[2 * j + 1];
         const R wr = pr - a * dr, wi = pi - a * di;
-        acc[0] += s.mult * ((double)pr * wr + (double)pi * wi);
+        acc[0].add((R)s.mult * (pr * wr + pi * wi));
         o[2 * j] = wr;
         o[2 * j + 1] = wi;
       }
@@ -194,10 +198,11 @@ __global__ void __launch_bounds__(kThreads)
   if constexpr (EPI == EPI_APPLYD) {
     return;
   } else if constexpr (EPI == EPI_SETUP) {
-    if (!grid_sum_last<4>(acc, ws)) return;
+    double sums[4] = {acc[0].value(), acc[1].value(), acc[2].value(), acc[3].value()};
+    if (!grid_sum_last<4>(sums, ws)) return;
     if (threadIdx.x == 0) {
       const double invNd = g.invN;
-      double dp = sqrt(acc[1] * invNd), snorm = sqrt(acc[0] * invNd);
+      double dp = sqrt(sums[1] * invNd), snorm = sqrt(sums[0] * invNd);
       if (snorm == 0.0) snorm = dp;
       sc->rnorm0 = snorm;
       sc->ttol = fmax(sc->rtol * snorm, sc->abstol);
@@ -206,17 +211,17 @@ __global__ void __launch_bounds__(kThreads)
       sc->iter = 0;
       sc->dpi = 0.0;
       sc->bcoef = 0.0;
-      sc->beta = acc[2] * invNd;
+      sc->beta = sums[2] * invNd;
       int st = conv_test(dp, sc);
       if (st == 0 && sc->beta == 0.0) {
         st = 2;
         sc->it = 1;
       }
       sc->status = st;
-      if (cx) sc->acc[6] += sc->kdot_weight * acc[3] * invNd;
+      if (cx) sc->acc[6] += sc->kdot_weight * sums[3] * invNd;
     }
   } else {
-    double a1[1] = {acc[0]};
+    double a1[1] = {acc[0].value()};
     if (!grid_sum_last<1>(a1, ws)) return;
     if (threadIdx.x == 0) {
       const double dpi = a1[0] * g.invN;
@@ -246,8 +251,8 @@ __global__ void __launch_bounds__(kThreads)
   const int64_t nvec = g.Ns * 2 / K;
   const R al = (R)sc->alpha;
   const R alN = (R)(sc->alpha * g.invN);
-  const double pcc = sc->pc_c;
-  double acc[2] = {0.0, 0.0};
+  const R pcc = (R)sc->pc_c;
+  Acc<R> acc[2];
   GRID_STRIDE(t, nvec) {
     R xv[K], pv[K], rv[K], wv[K];
     V::ld(x + t * K, xv);
@@ -262,21 +267,22 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
     for (int j = 0; j < CPV; j++) {
       SpecIdx s = spec_index((uint32_t)(t * CPV + j), g);
-      const double P = pc_mult(pcc, s.wx, s.wy, s.wz);
-      const double m2 = (double)rv[2 * j] * rv[2 * j] + (double)rv[2 * j + 1] * rv[2 * j + 1];
-      acc[0] += s.mult * P * P * m2;
-      acc[1] += s.mult * P * m2;
+      const R P = pc_mult<R>(pcc, s.wx, s.wy, s.wz);
+      const R m2 = (R)s.mult * (rv[2 * j] * rv[2 * j] + rv[2 * j + 1] * rv[2 * j + 1]);
+      acc[0].add(P * P * m2);
+      acc[1].add(P * m2);
     }
     V::st(x + t * K, xv);
     V::st(r + t * K, rv);
   }
-  if (!grid_sum_last<2>(acc, ws)) return;
+  double sums[2] = {acc[0].value(), acc[1].value()};
+  if (!grid_sum_last<2>(sums, ws)) return;
   if (threadIdx.x == 0) {
-    const double dp = sqrt(acc[0] * g.invN);
+    const double dp = sqrt(sums[0] * g.invN);
     sc->dp = dp;
     int st = conv_test(dp, sc);
     if (st == 0) {
-      const double bnew = acc[1] * g.invN;
+      const double bnew = sums[1] * g.invN;
       sc->beta = bnew;
       sc->bcoef = bnew / sc->beta_old;
       sc->iter = sc->iter + 1;
@@ -352,7 +358,7 @@ __global__ void __launch_bounds__(kThreads)
                    const R* __restrict__ csf, double weight, DevScalars* sc, RedWs ws) {
   using V = V16<R>;
   constexpr int K = V::K;
-  double acc[3] = {0.0, 0.0, 0.0};
+  Acc<R> acc[3];
   GRID_STRIDE(t, N / K) {
     R cv[K], av[K], w[K], gg[K], f[K];
     V::ld(c + t * K, cv);
@@ -362,15 +368,16 @@ __global__ void __launch_bounds__(kThreads)
     V::ld(csf + t * K, f);
 #pragma unroll
     for (int q = 0; q < K; q++) {
-      const double v = ((double)cv[q] * cv[q] - cv[q]) * av[q];
-      acc[0] += w[q] * v;
-      acc[1] += gg[q] * v;
-      acc[2] += f[q] * v;
+      const R v = (cv[q] * cv[q] - cv[q]) * av[q];
+      acc[0].add(w[q] * v);
+      acc[1].add(gg[q] * v);
+      acc[2].add(f[q] * v);
     }
   }
-  if (!grid_sum_last<3>(acc, ws)) return;
+  double sums[3] = {acc[0].value(), acc[1].value(), acc[2].value()};
+  if (!grid_sum_last<3>(sums, ws)) return;
   if (threadIdx.x == 0)
-    for (int q = 0; q < 3; q++) sc->acc[3 + q] += weight * acc[q];
+    for (int q = 0; q < 3; q++) sc->acc[3 + q] += weight * sums[q];
 }
 
 template <typename R>
@@ -380,7 +387,7 @@ __global__ void __launch_bounds__(kThreads)
                      const R* __restrict__ csf, double weight, DevScalars* sc, RedWs ws) {
   using V = V16<R>;
   constexpr int K = V::K;
-  double acc[3] = {0.0, 0.0, 0.0};
+  Acc<R> acc[3];
   GRID_STRIDE(t, N / K) {
     R c0[K], c1[K], c2[K], a0[K], a1[K], a2[K], w[K], gg[K], f[K];
     V::ld(gc3 + t * K, c0);
@@ -394,17 +401,18 @@ __global__ void __launch_bounds__(kThreads)
     V::ld(csf + t * K, f);
 #pragma unroll
     for (int q = 0; q < K; q++) {
-      double v = (double)c0[q] * a0[q];
-      v += (double)c1[q] * a1[q];
-      v += (double)c2[q] * a2[q];
-      acc[0] += w[q] * v;
-      acc[1] += gg[q] * v;
-      acc[2] += f[q] * v;
+      R v = c0[q] * a0[q];
+      v += c1[q] * a1[q];
+      v += c2[q] * a2[q];
+      acc[0].add(w[q] * v);
+      acc[1].add(gg[q] * v);
+      acc[2].add(f[q] * v);
     }
   }
-  if (!grid_sum_last<3>(acc, ws)) return;
+  double sums[3] = {acc[0].value(), acc[1].value(), acc[2].value()};
+  if (!grid_sum_last<3>(sums, ws)) return;
   if (threadIdx.x == 0)
-    for (int q = 0; q < 3; q++) sc->acc[q] += weight * acc[q];
+    for (int q = 0; q < 3; q++) sc->acc[q] += weight * sums[q];
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -418,7 +426,7 @@ __global__ void __launch_bounds__(kThreads)
                    const R* __restrict__ d, R* __restrict__ pt, DevScalars* sc, RedWs ws) {
   using V = V16<R>;
   constexpr int K = V::K;
-  double acc[1] = {0.0};
+  Acc<R> acc;
   GRID_STRIDE(t, N / K) {
     R cv[K], ov[K], dv[K], pv[K];
     V::ld(c + t * K, cv);
@@ -427,13 +435,14 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
     for (int q = 0; q < K; q++) {
       const R r = cv[q] * ov[q] - dv[q];
-      acc[0] += (double)r * r;
+      acc.add(r * r);
       pv[q] = -(r * ov[q]);
     }
     if (pt) V::st(pt + t * K, pv);
   }
-  if (!grid_sum_last<1>(acc, ws)) return;
-  if (threadIdx.x == 0) sc->red[0] = acc[0];
+  double sums[1] = {acc.value()};
+  if (!grid_sum_last<1>(sums, ws)) return;
+  if (threadIdx.x == 0) sc->red[0] = sums[0];
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -445,10 +454,11 @@ template <typename R>
 __global__ void __launch_bounds__(kThreads)
     k_dot(int64_t N, const R* __restrict__ x, const R* __restrict__ y, DevScalars* sc, int slot,
           RedWs ws) {
-  double acc[1] = {0.0};
-  GRID_STRIDE(i, N) { acc[0] += y ? (double)x[i] * (double)y[i] : (double)x[i]; }
-  if (!grid_sum_last<1>(acc, ws)) return;
-  if (threadIdx.x == 0) sc->red[slot] = acc[0];
+  Acc<R> acc;
+  GRID_STRIDE(i, N) { acc.add(y ? x[i] * y[i] : x[i]); }
+  double sums[1] = {acc.value()};
+  if (!grid_sum_last<1>(sums, ws)) return;
+  if (threadIdx.x == 0) sc->red[slot] = sums[0];
 }
 
 template <typename R>

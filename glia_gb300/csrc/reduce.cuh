@@ -79,6 +79,30 @@ __device__ __forceinline__ bool grid_sum_last(double (&v)[Q], RedWs ws) {
   return true;
 }
 
+// Per-thread accumulator. For float data the terms are summed in FP32 with Kahan compensation
+// (four FP32 operations per term, accurate to O(eps_32^2) of the summed magnitude), then widened
+// to FP64 for the warp / block / grid combine. This keeps the FP64 units, which are scarce on
+// GB300, out of the per-element path while the reduction stays at double-length accuracy.
+template <typename R>
+struct Acc;
+template <>
+struct Acc<float> {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+template <>
+struct Acc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+
 // 16-byte vector access to real arrays.
 template <typename R>
 struct V16;
