@@ -123,6 +123,8 @@ SIGNATURES = {
     "get_stats": (c_int, [_CTX, POINTER(GliaStats)]),
     "reset_stats": (c_int, [_CTX]),
     "set_timing": (c_int, [_CTX, c_int]),
+    "mismatch_f32_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p,
+                                     c_void_p]),
     "get_timing": (c_int, [_CTX, c_int, POINTER(c_char_p), POINTER(c_int64), POINTER(c_double),
                            POINTER(c_double)]),
 }

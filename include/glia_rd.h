@@ -199,6 +199,22 @@ int glia_set_timing(glia_ctx* ctx, int enable);
 int glia_get_timing(glia_ctx* ctx, int slot, const char** name, int64_t* launches, double* ms,
                     double* algorithmic_bytes);
 
+/* ---- data mismatch without allocation (extension; no counterpart in the reference) ---------
+ * For callers that cannot let a library allocate device memory: code that captures its loss
+ * evaluation into a CUDA graph (cudaMalloc is not allowed during stream capture), processes
+ * that run under a fixed device-memory budget held by their own allocator, and callers with no
+ * glia context. Computes *sumsq = sum_i (obs_i c_i - d_i)^2 (the ||O c(1) - d||^2 term of
+ * DerivativeOperatorsRD::evaluateObjective, before the h^3/2 factor) and, when pt is not NULL,
+ * pt_i = -obs_i (obs_i c_i - d_i) (the adjoint final condition). All pointers are device
+ * pointers (float fields, one double result); work is ordered on `stream` (NULL = the legacy
+ * default stream). It needs no context and calls no allocator: its reduction scratch is a
+ * static 64 KiB device array shared by every call, which limits n to 2^29 voxels (larger n
+ * returns GLIA_ERR_INVALID). The first call on each device resolves that array's address
+ * (cudaGetSymbolAddress) and must come before any stream capture. Calls that overlap on the GPU
+ * race on the shared scratch; serialise them. */
+int glia_mismatch_f32_noalloc(const float* c, const float* obs, const float* d, float* pt,
+                              int64_t n, double* sumsq, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
