@@ -49,6 +49,38 @@ static __global__ void k_solve_config(DevScalars* s, double a_cn, double pc_c, d
 static __global__ void k_acc_reset(DevScalars* s) {
   for (int q = 0; q < 8; q++) s->acc[q] = 0.0;
 }
+static __global__ void k_solve_stats_reset(DevScalars* s) {
+  s->sum_its[0] = s->sum_its[1] = s->sum_its[2] = 0;
+  s->nsolves = 0;
+  s->max_its = 0;
+  s->err_status = 0;
+  s->err_its = 0;
+  s->last_dp = 0.0;
+}
+// End of one diffusion solve: fold its PCG outcome into the sweep statistics.
+static __global__ void k_solve_finish(DevScalars* s, int which) {
+  const int it = s->it;
+  s->sum_its[which] += it;
+  s->nsolves += 1;
+  if (it > s->max_its) s->max_its = it;
+  s->last_dp = s->dp;
+  if (s->status < 0 && s->err_status == 0) {
+    s->err_status = s->status;
+    s->err_its = it;
+  }
+}
+// Head of the PCG graph: run the loop body only if the set-up left the solve unconverged.
+static __global__ void k_cond_set(DevScalars* s, cudaGraphConditionalHandle h) {
+  s->guard = 0;
+  cudaGraphSetConditional(h, s->status == 0 ? 1u : 0u);
+}
+// Tail of the loop body: continue while the PCG runs; the guard bounds the loop at maxit + 1
+// body executions whatever the scalars say.
+static __global__ void k_cond_step(DevScalars* s, cudaGraphConditionalHandle h) {
+  s->guard += 1;
+  if (s->status == 0 && s->guard > s->maxit) s->status = -3;
+  cudaGraphSetConditional(h, s->status == 0 ? 1u : 0u);
+}
 
 // Status summary read back after each PCG iteration (one 32-byte copy).
 struct SolveStatus {
@@ -105,6 +137,7 @@ class Engine final : public EngineBase {
 
   ~Engine() override {
     cudaStreamSynchronize(stream_);
+    if (cg_exec_) cudaGraphExecDestroy(cg_exec_);
     for (cufftHandle* p : {&r2c1_, &c2r1_, &r2c3_, &c2r3_})
       if (*p) cufftDestroy(*p);
     destroy_batch_plans();
@@ -255,13 +288,17 @@ class Engine final : public EngineBase {
     if (!(dt > 0)) throw Error(GLIA_ERR_INVALID, "diffusion_solve: dt must be > 0");
     import_field(c, tmp_);
     solve(tmp_, dt, nullptr, nullptr, 0.0);
+    sync_sweep();
     export_field(tmp_, c);
     return ksp_itr_;
   }
 
   // DiffusionSolver::solve (src/pde/DiffusionSolver.cpp:217-250). chat_slot receives F(c) (the
   // state spectrum, kept for the kappa gradient); cx/kdot_w add kdot_w * <cx, D c> to acc[6].
-  void solve(R* c, double dts, R* chat_slot, const R* cx, double kdot_w) {
+  // which: 0 state, 1 adjoint, 2 other (set-up, recomputation) for the iteration counters.
+  // The fused engine does not wait for the solve: its outcome is folded into device counters
+  // that sync_sweep() reads once per sweep.
+  void solve(R* c, double dts, R* chat_slot, const R* cx, double kdot_w, int which = 2) {
     ctx_dt_ = dts;
     if (pc_dt_mode_ == GLIA_PC_DT_MATCHED) prec_factor_dt(2.0 * dts);
     st_.total_diffusion_solves++;
@@ -270,13 +307,15 @@ class Engine final : public EngineBase {
       if (chat_slot) r2c(r2c1_, c, chat_slot);
       return;
     }
-    if (ref_)
+    if (ref_) {
       ref_solve(c, dts);
-    else
-      fused_solve(c, dts, chat_slot ? chat_slot : chat_, cx, kdot_w);
+      if (which < 2) (which == 0 ? st_.diff_ksp_itr_state : st_.diff_ksp_itr_adj) += ksp_itr_;
+    } else {
+      fused_solve(c, dts, chat_slot ? chat_slot : chat_, cx, kdot_w, which);
+    }
   }
 
-  void fused_solve(R* c, double dts, R* chat, const R* cx, double kdot_w) {
+  void fused_solve(R* c, double dts, R* chat, const R* cx, double kdot_w, int which) {
     k_solve_config<<<1, 1, 0, stream_>>>(sc_, 0.5 * dts, 0.25 * pc_dt_ * pc_kbar_, rtol_, abstol_,
                                          divtol_, maxit_, kdot_w);
     GLIA_LAUNCH_CHECK();
@@ -287,20 +326,112 @@ class Engine final : public EngineBase {
     GLIA_TIMED(KS_DIV_SETUP, SB() * (cx ? 7 : 6),
                k_spec_div<R, EPI_SETUP><<<red_blocks_, kThreads, 0, stream_>>>(
                    g_, g3s_, chat, cx, xhat_, rhat_, R(0), sc_, ws_));
-    SolveStatus s = read_status();
-    while (s.status == 0) {
-      launch_grad3<true>(rhat_, phat_);  // p = P r + b p, gradient spectra of p
-      apply_k_spectral();                // 3 C2R, k *, 3 R2C
-      GLIA_TIMED(KS_DIV_CGW, SB() * 5,
-                 k_spec_div<R, EPI_CGW><<<red_blocks_, kThreads, 0, stream_>>>(
-                     g_, g3s_, phat_, nullptr, what_, nullptr, R(0), sc_, ws_));
-      GLIA_TIMED(KS_CG_UPDATE, SB() * 6,
-                 k_cg_update<R><<<red_blocks_, kThreads, 0, stream_>>>(g_, xhat_, phat_, rhat_,
-                                                                       what_, sc_, ws_));
-      s = read_status();
+    if (use_graph()) {
+      GLIA_CUDA(cudaGraphLaunch(cg_exec_, stream_));  // the whole PCG loop, no host round trip
+    } else {
+      SolveStatus s = read_status();
+      while (s.status == 0) {
+        cg_iteration();
+        s = read_status();
+      }
     }
     c2r(c2r1_, xhat_, c);  // x = F^-1 (x')
-    finish_solve(s);
+    k_solve_finish<<<1, 1, 0, stream_>>>(sc_, which);
+    GLIA_LAUNCH_CHECK();
+  }
+
+  // one PCG iteration of the fused engine (launched directly, or captured as the loop body)
+  void cg_iteration() {
+    launch_grad3<true>(rhat_, phat_);  // p = P r + b p, gradient spectra of p
+    apply_k_spectral();                // 3 C2R, k *, 3 R2C
+    GLIA_TIMED(KS_DIV_CGW, SB() * 5,
+               k_spec_div<R, EPI_CGW><<<red_blocks_, kThreads, 0, stream_>>>(
+                   g_, g3s_, phat_, nullptr, what_, nullptr, R(0), sc_, ws_));
+    GLIA_TIMED(KS_CG_UPDATE, SB() * 6,
+               k_cg_update<R><<<red_blocks_, kThreads, 0, stream_>>>(g_, xhat_, phat_, rhat_,
+                                                                     what_, sc_, ws_));
+  }
+
+  // The PCG loop as one CUDA graph: [k_cond_set] -> WHILE(cond) { iteration; k_cond_step }.
+  // All buffers and scalars it touches are fixed per engine, so one instantiation serves every
+  // solve. If the graph cannot be built, the host-driven loop is used instead.
+  bool use_graph() {
+    if (tm_.on || graph_state_ < 0) return false;
+    if (graph_state_ == 0) build_cg_graph();
+    return graph_state_ > 0;
+  }
+  void build_cg_graph() {
+    cudaGraph_t g = nullptr;
+    cudaStream_t cs = nullptr;
+    cudaStream_t saved = stream_;
+    bool capturing = false;
+    try {
+      GLIA_CUDA(cudaGraphCreate(&g, 0));
+      cudaGraphConditionalHandle h;
+      GLIA_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+      DevScalars* scp = sc_;
+      void* args_set[] = {&scp, &h};
+      cudaKernelNodeParams kp = {};
+      kp.func = (void*)k_cond_set;
+      kp.gridDim = dim3(1);
+      kp.blockDim = dim3(1);
+      kp.kernelParams = args_set;
+      cudaGraphNode_t head;
+      GLIA_CUDA(cudaGraphAddKernelNode(&head, g, nullptr, 0, &kp));
+      cudaGraphNodeParams cp = {};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = h;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      cudaGraphNode_t loop;
+      GLIA_CUDA(cudaGraphAddNode(&loop, g, &head, nullptr, 1, &cp));
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      GLIA_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+      for (cufftHandle p : {r2c3_, c2r3_}) GLIA_CUFFT(cufftSetStream(p, cs));
+      stream_ = cs;
+      GLIA_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal));
+      capturing = true;
+      cg_iteration();
+      k_cond_step<<<1, 1, 0, cs>>>(sc_, h);
+      GLIA_LAUNCH_CHECK();
+      cudaGraph_t captured = nullptr;
+      capturing = false;
+      GLIA_CUDA(cudaStreamEndCapture(cs, &captured));
+      GLIA_CUDA(cudaGraphInstantiate(&cg_exec_, g, 0));
+      graph_state_ = 1;
+    } catch (const Error&) {
+      if (capturing) {
+        cudaGraph_t junk = nullptr;
+        cudaStreamEndCapture(cs, &junk);
+      }
+      cudaGetLastError();
+      cg_exec_ = nullptr;
+      graph_state_ = -1;
+    }
+    stream_ = saved;
+    for (cufftHandle p : {r2c3_, c2r3_}) cufftSetStream(p, stream_);
+    if (cs) cudaStreamDestroy(cs);
+    if (g) cudaGraphDestroy(g);
+  }
+
+  // Reads the device-side solve statistics of the sweep and reports the first failed solve.
+  void sync_sweep() {
+    if (ref_) return;
+    GLIA_CUDA(cudaMemcpyAsync(hsc_, sc_, sizeof(DevScalars), cudaMemcpyDeviceToHost, stream_));
+    GLIA_CUDA(cudaStreamSynchronize(stream_));
+    tm_.harvest();
+    const DevScalars& h = *hsc_;
+    st_.diff_ksp_itr_state += h.sum_its[0];
+    st_.diff_ksp_itr_adj += h.sum_its[1];
+    st_.total_pcg_iterations += h.sum_its[0] + h.sum_its[1] + h.sum_its[2];
+    st_.max_ksp_itr = std::max(st_.max_ksp_itr, h.max_its);
+    st_.last_rnorm = h.last_dp;
+    st_.last_ksp_itr = h.it;
+    ksp_itr_ = h.it;
+    k_solve_stats_reset<<<1, 1, 0, stream_>>>(sc_);
+    GLIA_LAUNCH_CHECK();
+    if (h.err_status < 0) finish_solve(SolveStatus{h.err_status, h.err_its, h.last_dp});
   }
 
   template <bool CGDIR>
@@ -747,16 +878,13 @@ class Engine final : public EngineBase {
   // One splitting step from the state in `c` (PdeOperatorsRD::solveState loop body,
   // src/pde/PdeOperators.cpp:260-300). chat_slot: spectrum of c before the step; half_out:
   // state after the first diffusion sub-step.
-  void step(R* c, R* chat_slot, R* half_out) {
+  void step(R* c, R* chat_slot, R* half_out, int which = 0) {
     if (order_ == 2) {
-      solve(c, dt_ / 2.0, chat_slot, nullptr, 0.0);
-      st_.diff_ksp_itr_state += ksp_itr_;
+      solve(c, dt_ / 2.0, chat_slot, nullptr, 0.0, which);
       reaction(c, half_out);
-      solve(c, dt_ / 2.0, nullptr, nullptr, 0.0);
-      st_.diff_ksp_itr_state += ksp_itr_;
+      solve(c, dt_ / 2.0, nullptr, nullptr, 0.0, which);
     } else {
-      solve(c, dt_, chat_slot, nullptr, 0.0);
-      st_.diff_ksp_itr_state += ksp_itr_;
+      solve(c, dt_, chat_slot, nullptr, 0.0, which);
       reaction(c, half_out);
     }
   }
@@ -787,6 +915,7 @@ class Engine final : public EngineBase {
         step(ct_, nullptr, nullptr);
       }
     }
+    sync_sweep();
     state_done_ = true;
     adjoint_done_ = false;
     trick_at_state_ = trick;
@@ -803,14 +932,11 @@ class Engine final : public EngineBase {
     const double w = (i + 1 == nt_) ? 0.5 : 1.0;
     const R* cxx = accumulate ? cx : nullptr;
     if (order_ == 2) {
-      solve(p0_, dt_ / 2.0, nullptr, cxx, w * dt_);
-      st_.diff_ksp_itr_adj += ksp_itr_;
+      solve(p0_, dt_ / 2.0, nullptr, cxx, w * dt_, 1);
       reaction_adjoint(chalf);
-      solve(p0_, dt_ / 2.0, nullptr, nullptr, 0.0);
-      st_.diff_ksp_itr_adj += ksp_itr_;
+      solve(p0_, dt_ / 2.0, nullptr, nullptr, 0.0, 1);
     } else {
-      solve(p0_, dt_, nullptr, cxx, w * dt_);
-      st_.diff_ksp_itr_adj += ksp_itr_;
+      solve(p0_, dt_, nullptr, cxx, w * dt_, 1);
       reaction_adjoint(chalf);
     }
   }
@@ -822,8 +948,7 @@ class Engine final : public EngineBase {
   // reactionAdjoint without stored half steps (src/pde/PdeOperators.cpp:331-344)
   const R* recompute_half(const R* ci) {
     vcopy(tmp_, ci);
-    solve(tmp_, order_ == 2 ? dt_ / 2.0 : dt_, nullptr, nullptr, 0.0);
-    st_.diff_ksp_itr_adj += ksp_itr_;
+    solve(tmp_, order_ == 2 ? dt_ / 2.0 : dt_, nullptr, nullptr, 0.0, 1);
     return tmp_;
   }
   // per-time-point gradient terms at time point i (state c_i, adjoint alpha_i in p0_)
@@ -877,16 +1002,13 @@ class Engine final : public EngineBase {
         const R* chalf = c_half_.empty() ? nullptr : c_half_[i];
         if (order_ == 2) {
           solve(p0_, dt_ / 2.0, nullptr, (accumulate && trick) ? chat_hist_[i + 1] : nullptr,
-                ((i + 1 == nt_) ? 0.5 : 1.0) * dt_);
-          st_.diff_ksp_itr_adj += ksp_itr_;
+                ((i + 1 == nt_) ? 0.5 : 1.0) * dt_, 1);
           if (!chalf) chalf = recompute_half(c_hist_[i]);
           reaction_adjoint(chalf);
-          solve(p0_, dt_ / 2.0, nullptr, nullptr, 0.0);
-          st_.diff_ksp_itr_adj += ksp_itr_;
+          solve(p0_, dt_ / 2.0, nullptr, nullptr, 0.0, 1);
         } else {
           solve(p0_, dt_, nullptr, (accumulate && trick) ? chat_hist_[i + 1] : nullptr,
-                ((i + 1 == nt_) ? 0.5 : 1.0) * dt_);
-          st_.diff_ksp_itr_adj += ksp_itr_;
+                ((i + 1 == nt_) ? 0.5 : 1.0) * dt_, 1);
           if (!chalf) chalf = recompute_half(c_hist_[i]);
           reaction_adjoint(chalf);
         }
@@ -903,9 +1025,8 @@ class Engine final : public EngineBase {
         vcopy(seg_c_[0], ckpt_[s]);
         vcopy(tmp2(), ckpt_[s]);
         for (int i = i0; i < i1; i++) {
-          const int64_t ks = st_.diff_ksp_itr_state;
-          step(tmp2(), trick ? seg_chat_[i - i0] : nullptr, seg_half_[i - i0]);
-          st_.diff_ksp_itr_state = ks;  // recompute solves are not state solves
+          // recompute solves are neither state nor adjoint solves (which = 2)
+          step(tmp2(), trick ? seg_chat_[i - i0] : nullptr, seg_half_[i - i0], 2);
           vcopy(seg_c_[i - i0 + 1], tmp2());
         }
         if (trick) r2c(r2c1_, tmp2(), seg_chat_[i1 - i0]);
@@ -917,6 +1038,7 @@ class Engine final : public EngineBase {
         if (s == 0 && accumulate && trick) kappa_dot_at(seg_chat_[0], 0.5 * dt_);
       }
     }
+    sync_sweep();
     adjoint_done_ = true;
   }
   R* tmp2() {
@@ -1306,6 +1428,8 @@ class Engine final : public EngineBase {
   std::unordered_map<void*, size_t> sizes_;
   int64_t bytes_ = 0;
   KTimer tm_;
+  int graph_state_ = 0;  // 0 not built, 1 built, -1 unavailable (host-driven loop)
+  cudaGraphExec_t cg_exec_ = nullptr;
 
   cufftHandle r2c1_ = 0, c2r1_ = 0, r2c3_ = 0, c2r3_ = 0, r2cB_ = 0, c2rB_ = 0;
   char* fft_ws_ = nullptr;

@@ -31,6 +31,14 @@ struct DevScalars {
   double kdot_weight;  // weight of the next <c, D alpha> contribution
   double acc[8];       // [0..2] kappa (wm, gm, csf) explicit, [3..5] rho, [6] kappa via <c, D a>
   double red[4];       // generic reduction results
+  // per-sweep solve statistics, accumulated on the device (read once per sweep)
+  long long sum_its[3];  // PCG iterations of state / adjoint / other solves
+  long long nsolves;
+  int max_its;
+  int err_status;        // first failing solve's status (0 = none)
+  int err_its;
+  int guard;             // WHILE-loop body executions of the current solve
+  double last_dp;
 };
 
 __device__ __forceinline__ int conv_test(double rn, const DevScalars* s) {

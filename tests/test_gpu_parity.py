@@ -158,3 +158,24 @@ def test_gradient_matches_central_differences():
         h = 1e-3
         fd = (g.eval_objective(x + h * d, d1) - g.eval_objective(x - h * d, d1)) / (2 * h)
         assert abs(fd - gr @ d) <= 1e-4 * max(abs(fd), 1e-12), (fd, gr @ d)
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+def test_graph_loop_equals_host_loop(prec):
+    """The PCG loop as a CUDA graph with a device-side WHILE node gives the same bits as the
+    host-driven loop (used while per-kernel timing is on)."""
+    n, nt = 32, 4
+    wl, tissue, centers = small_problem(n, nt)
+    d1 = observation(wl, tissue, centers)
+    x = np.concatenate([np.linspace(0.1, 0.9, len(centers)), [wl.kappa, wl.rho]])
+    out = []
+    for timing in (False, True):
+        g = gpu(n, prec)
+        configure(g, wl, tissue, centers)
+        g.set_obs_filter(np.ones(n ** 3))
+        g.set_timing(timing)
+        out.append(g.eval_objective_and_gradient(x, d1) + (g.stats(),))
+    (J0, g0, s0), (J1, g1, s1) = out
+    assert J0 == J1 and np.array_equal(g0, g1)
+    assert s0["diff_ksp_itr_state"] == s1["diff_ksp_itr_state"]
+    assert s0["diff_ksp_itr_adj"] == s1["diff_ksp_itr_adj"]
