@@ -328,6 +328,7 @@ class Engine final : public EngineBase {
                    g_, g3s_, chat, cx, xhat_, rhat_, R(0), sc_, ws_));
     if (use_graph()) {
       GLIA_CUDA(cudaGraphLaunch(cg_exec_, stream_));  // the whole PCG loop, no host round trip
+      graph_solves_ = true;
     } else {
       SolveStatus s = read_status();
       while (s.status == 0) {
@@ -425,6 +426,9 @@ class Engine final : public EngineBase {
     st_.diff_ksp_itr_state += h.sum_its[0];
     st_.diff_ksp_itr_adj += h.sum_its[1];
     st_.total_pcg_iterations += h.sum_its[0] + h.sum_its[1] + h.sum_its[2];
+    // transforms launched inside the PCG graph: 3 C2R + 3 R2C per iteration
+    if (graph_solves_) st_.total_fft_execs += 6 * (h.sum_its[0] + h.sum_its[1] + h.sum_its[2]);
+    graph_solves_ = false;
     st_.max_ksp_itr = std::max(st_.max_ksp_itr, h.max_its);
     st_.last_rnorm = h.last_dp;
     st_.last_ksp_itr = h.it;
@@ -1429,6 +1433,7 @@ class Engine final : public EngineBase {
   int64_t bytes_ = 0;
   KTimer tm_;
   int graph_state_ = 0;  // 0 not built, 1 built, -1 unavailable (host-driven loop)
+  bool graph_solves_ = false;  // the current sweep ran PCG loops as graphs
   cudaGraphExec_t cg_exec_ = nullptr;
 
   cufftHandle r2c1_ = 0, c2r1_ = 0, r2c3_ = 0, c2r3_ = 0, r2cB_ = 0, c2rB_ = 0;
