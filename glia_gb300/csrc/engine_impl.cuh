@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 #include <unordered_map>
@@ -22,6 +23,7 @@
 #include "engine.hpp"
 #include "kernels.cuh"
 #include "ktimer.cuh"
+#include "zpass.cuh"
 
 #define GLIA_TIMED(slot, bytes, ...)             \
   do {                                           \
@@ -138,7 +140,7 @@ class Engine final : public EngineBase {
   ~Engine() override {
     cudaStreamSynchronize(stream_);
     if (cg_exec_) cudaGraphExecDestroy(cg_exec_);
-    for (cufftHandle* p : {&r2c1_, &c2r1_, &r2c3_, &c2r3_})
+    for (cufftHandle* p : {&r2c1_, &c2r1_, &r2c3_, &c2r3_, &p2d_})
       if (*p) cufftDestroy(*p);
     destroy_batch_plans();
     for (auto& kv : sizes_) cudaFree(kv.first);
@@ -158,6 +160,7 @@ class Engine final : public EngineBase {
   void set_stream(void* s) override {
     stream_ = s ? (cudaStream_t)s : own_stream_;
     for (cufftHandle p : {r2c1_, c2r1_, r2c3_, c2r3_}) GLIA_CUFFT(cufftSetStream(p, stream_));
+    if (zpass_) GLIA_CUFFT(cufftSetStream(p2d_, stream_));
   }
   void synchronize() override { GLIA_CUDA(cudaStreamSynchronize(stream_)); }
   int64_t device_bytes() const override { return bytes_; }
@@ -389,6 +392,7 @@ class Engine final : public EngineBase {
       cudaGraph_t body = cp.conditional.phGraph_out[0];
       GLIA_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
       for (cufftHandle p : {r2c3_, c2r3_}) GLIA_CUFFT(cufftSetStream(p, cs));
+      if (zpass_) GLIA_CUFFT(cufftSetStream(p2d_, cs));
       stream_ = cs;
       GLIA_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
                                               cudaStreamCaptureModeThreadLocal));
@@ -412,6 +416,7 @@ class Engine final : public EngineBase {
     }
     stream_ = saved;
     for (cufftHandle p : {r2c3_, c2r3_}) cufftSetStream(p, stream_);
+    if (zpass_) cufftSetStream(p2d_, stream_);
     if (cs) cudaStreamDestroy(cs);
     if (g) cudaGraphDestroy(g);
   }
@@ -444,8 +449,18 @@ class Engine final : public EngineBase {
                k_spec_grad3<R, CGDIR><<<pw_blocks_, kThreads, 0, stream_>>>(g_, src, pdir, g3s_,
                                                                             sc_));
   }
-  // gradient spectra (g3s_) -> real gradient -> times k -> spectra of k * grad (g3s_)
+  // gradient spectra (g3s_) -> real gradient -> times k -> spectra of k * grad (g3s_).
+  // FP32 with n = 64 ... 512: cuFFT does the (x, y) passes in place and k_zpass_mulk the fused
+  // z pass; otherwise three-dimensional cuFFT transforms around k_mul_k3.
   void apply_k_spectral() {
+    if (zpass_) {
+      for (int j = 0; j < 3; j++) c2c2d(g3s_ + j * 2 * Ns_, CUFFT_INVERSE);
+      const int lines = g_.n * g_.n;
+      const int blocks = std::min((lines + kWarps - 1) / kWarps, sms_ * 8);
+      GLIA_TIMED(KS_ZPASS, SB() * 6 + FB(), launch_zpass(blocks, lines));
+      for (int j = 0; j < 3; j++) c2c2d(g3s_ + j * 2 * Ns_, CUFFT_FORWARD);
+      return;
+    }
     c2r(c2r3_, g3s_, g3r_, 3);
     GLIA_TIMED(KS_MUL_K3, FB() * 7,
                k_mul_k3<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, g3r_, kxx_, sc_, 0));
@@ -1277,14 +1292,62 @@ class Engine final : public EngineBase {
     return p;
   }
   void make_plans() {
-    size_t w[4] = {0, 0, 0, 0};
+    size_t w[5] = {0, 0, 0, 0, 0};
     r2c1_ = make_plan(CT<R>::kR2C, 1, &w[0]);
     c2r1_ = make_plan(CT<R>::kC2R, 1, &w[1]);
     r2c3_ = make_plan(CT<R>::kR2C, 3, &w[2]);
     c2r3_ = make_plan(CT<R>::kC2R, 3, &w[3]);
-    fft_ws_bytes_ = std::max({w[0], w[1], w[2], w[3], (size_t)16});
+    const int n = g_.n;
+    const char* off = std::getenv("GLIA_DISABLE_ZPASS");
+    zpass_ = std::is_same<R, float>::value && (n == 64 || n == 128 || n == 256 || n == 512) &&
+             !(off && off[0] == '1') && !ref_;
+    if (zpass_) {
+      // 2-D C2C over (x, y) for every kz: element (x, y, kz) at (x n + y)(n/2+1) + kz
+      GLIA_CUFFT(cufftCreate(&p2d_));
+      GLIA_CUFFT(cufftSetAutoAllocation(p2d_, 0));
+      int dims[2] = {n, n}, emb[2] = {n, n};
+      GLIA_CUFFT(cufftMakePlanMany(p2d_, 2, dims, emb, g_.nh, 1, emb, g_.nh, 1, CUFFT_C2C, g_.nh,
+                                   &w[4]));
+      GLIA_CUFFT(cufftSetStream(p2d_, stream_));
+      // twiddles W_n^j = exp(-2 pi i j / n), j < n, in double precision on the host
+      std::vector<float2> tw(n);
+      for (int j = 0; j < n; j++) {
+        const double a = -2.0 * M_PI * (double)j / (double)n;
+        tw[j] = make_float2((float)std::cos(a), (float)std::sin(a));
+      }
+      tw_ = dalloc<float2>(n);
+      GLIA_CUDA(cudaMemcpyAsync(tw_, tw.data(), n * sizeof(float2), cudaMemcpyHostToDevice,
+                                stream_));
+      GLIA_CUDA(cudaStreamSynchronize(stream_));
+    }
+    fft_ws_bytes_ = std::max({w[0], w[1], w[2], w[3], w[4], (size_t)16});
     fft_ws_ = dalloc<char>((int64_t)fft_ws_bytes_);
     for (cufftHandle p : {r2c1_, c2r1_, r2c3_, c2r3_}) GLIA_CUFFT(cufftSetWorkArea(p, fft_ws_));
+    if (zpass_) GLIA_CUFFT(cufftSetWorkArea(p2d_, fft_ws_));
+  }
+  void c2c2d(R* data, int dir) {
+    cudaEvent_t ev = tm_.begin(stream_);
+    if constexpr (std::is_same<R, float>::value) {
+      cufftComplex* d = reinterpret_cast<cufftComplex*>(data);
+      GLIA_CUFFT(cufftExecC2C(p2d_, d, d, dir));
+    }
+    tm_.end(KS_FFT_2D, ev, 2.0 * SB(), stream_);
+    st_.total_fft_execs += 1;
+  }
+  void launch_zpass(int blocks, int lines) {
+    if constexpr (std::is_same<R, float>::value) {
+      const int n = g_.n;
+      float* s3 = g3s_;
+      const float* k = kxx_;
+      if (n == 64)
+        k_zpass_mulk<1><<<blocks, kThreads, 0, stream_>>>(n, lines, s3, Ns_, k, tw_);
+      else if (n == 128)
+        k_zpass_mulk<2><<<blocks, kThreads, 0, stream_>>>(n, lines, s3, Ns_, k, tw_);
+      else if (n == 256)
+        k_zpass_mulk<4><<<blocks, kThreads, 0, stream_>>>(n, lines, s3, Ns_, k, tw_);
+      else
+        k_zpass_mulk<8><<<blocks, kThreads, 0, stream_>>>(n, lines, s3, Ns_, k, tw_);
+    }
   }
   void ensure_batch_plans(int B) {
     destroy_batch_plans();
@@ -1436,7 +1499,9 @@ class Engine final : public EngineBase {
   bool graph_solves_ = false;  // the current sweep ran PCG loops as graphs
   cudaGraphExec_t cg_exec_ = nullptr;
 
-  cufftHandle r2c1_ = 0, c2r1_ = 0, r2c3_ = 0, c2r3_ = 0, r2cB_ = 0, c2rB_ = 0;
+  cufftHandle r2c1_ = 0, c2r1_ = 0, r2c3_ = 0, c2r3_ = 0, r2cB_ = 0, c2rB_ = 0, p2d_ = 0;
+  bool zpass_ = false;   // fused z pass (FP32, n = 64 ... 512)
+  float2* tw_ = nullptr;
   char* fft_ws_ = nullptr;
   char* batch_ws_ = nullptr;
   size_t fft_ws_bytes_ = 0;

@@ -33,6 +33,8 @@ enum KSlot {
   KS_FFT_C2R3,           // cuFFT C2R/Z2D, batch of 3
   KS_REF_VEC,            // reference-structured vector kernels (axpy, pointwise, wave number)
   KS_REF_DOT,            // reference-structured inner products
+  KS_ZPASS,              // k_zpass_mulk: fused z C2R, k multiply, z R2C
+  KS_FFT_2D,             // cuFFT 2-D C2C over (x, y) for every kz
   KS_COUNT
 };
 
@@ -41,7 +43,8 @@ static const char* const kSlotNames[KS_COUNT] = {
     "k_spec_div_cgw",     "k_spec_div_applyd", "k_cg_update",   "k_reaction_fwd",
     "k_reaction_lin",     "k_grad_acc",     "k_obs_residual",  "k_phi",
     "copy_d2d",           "cufft_r2c",      "cufft_c2r",       "cufft_r2c_x3",
-    "cufft_c2r_x3",       "ref_vector_ops", "ref_dot"};
+    "cufft_c2r_x3",       "ref_vector_ops", "ref_dot",         "k_zpass_mulk",
+    "cufft_c2c_2d"};
 
 struct KTimer {
   bool on = false;

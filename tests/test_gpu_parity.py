@@ -179,3 +179,40 @@ def test_graph_loop_equals_host_loop(prec):
     assert J0 == J1 and np.array_equal(g0, g1)
     assert s0["diff_ksp_itr_state"] == s1["diff_ksp_itr_state"]
     assert s0["diff_ksp_itr_adj"] == s1["diff_ksp_itr_adj"]
+
+
+@pytest.mark.parametrize("n", [64, 128, 256])
+def test_fused_zpass_matches_cufft_3d_path(n, monkeypatch):
+    """FP32 D apply with the fused z pass (k_zpass_mulk between 2-D cuFFT passes) against the
+    three-dimensional cuFFT transforms around k_mul_k3."""
+    wl, tissue, centers = small_problem(n, 2, n_gauss=8)
+    f = reference_test_field(n) + 0.1 * tissue.wm.reshape(-1)
+    out = []
+    for off in ("0", "1"):
+        monkeypatch.setenv("GLIA_DISABLE_ZPASS", off)
+        g = gpu(n, MIXED)
+        configure(g, wl, tissue, centers)
+        out.append((g.apply_d(f), g.solve_state(g.phi_apply(np.linspace(0.2, 1, 8)))))
+    assert rel_l2(out[0][0], out[1][0]) < 2e-6
+    assert rel_l2(out[0][1], out[1][1]) < 1e-5
+
+
+@pytest.mark.parametrize("n", [64, 128])
+def test_fused_zpass_against_oracle(n):
+    nt = 4
+    wl, tissue, centers = small_problem(n, nt, n_gauss=8)
+    o, g = orc(n), gpu(n, MIXED)
+    for ctx in (o, g):
+        configure(ctx, wl, tissue, centers)
+    f = reference_test_field(n) + 0.1 * tissue.wm.reshape(-1)
+    assert rel_l2(g.apply_d(f), o.apply_d(f)) < 2e-5
+    p = np.linspace(0.2, 1.0, len(centers))
+    c0 = o.phi_apply(p)
+    assert rel_l2(g.solve_state(c0), o.solve_state(c0)) < STATE_TOL[MIXED]
+    d1 = observation(wl, tissue, centers)
+    for ctx in (o, g):
+        ctx.set_obs_filter(np.ones(n ** 3))
+    x = np.concatenate([p, [wl.kappa, wl.rho]])
+    _, gro = o.eval_objective_and_gradient(x, d1)
+    _, grg = g.eval_objective_and_gradient(x, d1)
+    assert rel_l2(grg, gro) < GRAD_TOL
