@@ -188,8 +188,8 @@ def test_fused_zpass_matches_cufft_3d_path(n, monkeypatch):
     wl, tissue, centers = small_problem(n, 2, n_gauss=8)
     f = reference_test_field(n) + 0.1 * tissue.wm.reshape(-1)
     out = []
-    for off in ("0", "1"):
-        monkeypatch.setenv("GLIA_DISABLE_ZPASS", off)
+    for on in ("1", "0"):
+        monkeypatch.setenv("GLIA_ZPASS", on)
         g = gpu(n, MIXED)
         configure(g, wl, tissue, centers)
         out.append((g.apply_d(f), g.solve_state(g.phi_apply(np.linspace(0.2, 1, 8)))))
@@ -198,7 +198,8 @@ def test_fused_zpass_matches_cufft_3d_path(n, monkeypatch):
 
 
 @pytest.mark.parametrize("n", [64, 128])
-def test_fused_zpass_against_oracle(n):
+def test_fused_zpass_against_oracle(n, monkeypatch):
+    monkeypatch.setenv("GLIA_ZPASS", "1")
     nt = 4
     wl, tissue, centers = small_problem(n, nt, n_gauss=8)
     o, g = orc(n), gpu(n, MIXED)
