@@ -1,0 +1,211 @@
+"""Bounded L-BFGS inversion over (p, kappa, rho), the caller of the gradient path.
+
+Restates the reference's optimizer set-up (src/opt/Optimizer.cpp:116-286,
+src/opt/TILOptimizer.cpp:245-272, src/opt/TaoInterface.cpp:362-530): TAO BLMVM (bounded
+limited-memory variable metric) with 10 correction pairs, at most 10 function evaluations per line
+search, stopping when the projected-gradient norm falls below gttol * ||g_0|| (gttol = 1e-3) or
+below gatol (1e-4), or after newton_maxit (30) iterations; bounds p >= 0, kappa in [1e-3, 1],
+rho in [1, 15]. The search direction is the two-loop L-BFGS product with the scalar initial
+scaling s'y / y'y, projected onto the free variables; the step is a projected backtracking
+(Armijo) line search along P(x + a d). All vectors are FP64 on the host; each objective and
+gradient is one glia_eval_objective[_and_gradient] call.
+
+    python -m glia_gb300.inversion --n 128      # the 128^3 reconstruction, mixed vs FP64
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class LbfgsSettings:
+    m: int = 10                 # lbfgs_vectors_
+    gttol: float = 1e-3         # opttolgrad_: ||g|| < gttol ||g0||
+    gatol: float = 1e-4         # gatol_
+    maxit: int = 30             # newton_maxit_
+    ls_max_funcs: int = 10      # ls_max_func_evals
+    armijo_c1: float = 1e-4
+    shrink: float = 0.5
+
+
+@dataclass
+class LbfgsResult:
+    x: np.ndarray
+    J: float
+    gnorm: float
+    gnorm0: float
+    iterations: int
+    fevals: int
+    gevals: int
+    reason: str
+    history: list = field(default_factory=list)
+
+
+def projected_gradient(x, g, lb, ub):
+    pg = g.copy()
+    pg[(x <= lb) & (g > 0)] = 0.0
+    pg[(x >= ub) & (g < 0)] = 0.0
+    return pg
+
+
+def bounded_lbfgs(fun_grad, fun, x0, lb, ub, s: LbfgsSettings = LbfgsSettings()) -> LbfgsResult:
+    """Minimise fun over lb <= x <= ub. fun_grad(x) -> (J, g); fun(x) -> J."""
+    x = np.clip(np.asarray(x0, dtype=np.float64), lb, ub)
+    J, g = fun_grad(x)
+    fevals = gevals = 1
+    pg = projected_gradient(x, g, lb, ub)
+    g0 = float(np.linalg.norm(pg)) or 1.0
+    S, Y = [], []
+    hist = [{"it": 0, "J": J, "gnorm": g0}]
+    reason = "maxit"
+    it = 0
+    for it in range(1, s.maxit + 1):
+        gn = float(np.linalg.norm(pg))
+        if gn < s.gttol * g0:
+            reason = "gttol"
+            it -= 1
+            break
+        if gn < s.gatol:
+            reason = "gatol"
+            it -= 1
+            break
+        # two-loop recursion on the projected gradient
+        q = pg.copy()
+        alphas = []
+        for sv, yv in reversed(list(zip(S, Y))):
+            rho = 1.0 / (yv @ sv)
+            a = rho * (sv @ q)
+            q -= a * yv
+            alphas.append((rho, a))
+        gamma = (S[-1] @ Y[-1]) / (Y[-1] @ Y[-1]) if S else 1.0 / max(gn, 1e-300)
+        r = gamma * q
+        for (sv, yv), (rho, a) in zip(zip(S, Y), reversed(alphas)):
+            b = rho * (yv @ r)
+            r += (a - b) * sv
+        d = -r
+        # variables held at a bound by the gradient, or that the step would push out of the box
+        binding = ((x <= lb) & (g > 0)) | ((x >= ub) & (g < 0))
+        active = binding | ((x <= lb) & (d < 0)) | ((x >= ub) & (d > 0))
+        d[active] = 0.0
+        if not d @ pg < 0:  # not a descent direction: restart from the projected gradient
+            S.clear()
+            Y.clear()
+            d = -pg / max(gn, 1e-300)
+        # projected backtracking line search; the first trial also takes the gradient (it is
+        # accepted in most iterations), later trials take the objective only
+        step, accepted, gnew = 1.0, False, None
+        for trial in range(s.ls_max_funcs):
+            xn = np.clip(x + step * d, lb, ub)
+            if trial == 0:
+                Jn, gnew = fun_grad(xn)
+                gevals += 1
+            else:
+                Jn, gnew = fun(xn), None
+            fevals += 1
+            if Jn <= J + s.armijo_c1 * (g @ (xn - x)):
+                accepted = True
+                break
+            step *= s.shrink
+        if not accepted:
+            reason = "linesearch"
+            break
+        if gnew is None:
+            Jn, gnew = fun_grad(xn)
+            fevals += 1
+            gevals += 1
+        sv, yv = xn - x, gnew - g
+        if sv @ yv > 1e-12 * np.linalg.norm(sv) * np.linalg.norm(yv):
+            S.append(sv)
+            Y.append(yv)
+            if len(S) > s.m:
+                S.pop(0)
+                Y.pop(0)
+        x, J, g = xn, Jn, gnew
+        pg = projected_gradient(x, g, lb, ub)
+        hist.append({"it": it, "J": J, "gnorm": float(np.linalg.norm(pg)), "step": step})
+    return LbfgsResult(x=x, J=J, gnorm=float(np.linalg.norm(pg)), gnorm0=g0, iterations=it,
+                       fevals=fevals, gevals=gevals, reason=reason, history=hist)
+
+
+def reference_bounds(np_: int, k_lb=1e-3, k_ub=1.0, rho_lb=1.0, rho_ub=15.0):
+    """TILOptimizer::setVariableBounds / RDOptimizer bounds for x = [p, kappa, rho]."""
+    lb = np.concatenate([np.zeros(np_), [k_lb, rho_lb]])
+    ub = np.concatenate([np.full(np_, np.inf), [k_ub, rho_ub]])
+    return lb, ub
+
+
+def invert(ctx, d1, x0, lb, ub, settings: LbfgsSettings = LbfgsSettings()) -> LbfgsResult:
+    """L-BFGS on a configured context (objective = DerivativeOperatorsRD with all_gradients)."""
+    return bounded_lbfgs(lambda x: ctx.eval_objective_and_gradient(x, d1),
+                         lambda x: ctx.eval_objective(x, d1), x0, lb, ub, settings)
+
+
+# ------------------------------------------------------------------------------------------
+def reconstruction_problem(n=128, nt=40, seed_truth=4, seed_noise=5):
+    """The 128^3 reconstruction: 216 Gaussians on the reference's even 6x6x6 lattice (spacing
+    1.5 sigma around (pi, pi, pi)), truth with 3 active Gaussians (U[0.5, 1]), rho = 12,
+    kappa = 0.03, dt = 0.01, data = forward + N(0, 0.01^2)."""
+    from . import synthetic as syn
+    from .context import phi_mesh
+    from .native import load
+
+    tissue = syn.make_tissue(n, 0)
+    sigma = 2 * np.pi / 64
+    centers = phi_mesh(load(), 216, [np.pi, np.pi, np.pi], sigma, 1.5)
+    rng = np.random.default_rng(seed_truth)
+    p = np.zeros(216)
+    act = rng.choice(216, size=3, replace=False)
+    p[act] = rng.uniform(0.5, 1.0, size=3)
+    wl = syn.GradientWorkload(n=n, nt=nt, n_gauss=216, rho=12.0, kappa=0.03)
+    return wl, tissue, centers, np.concatenate([p, [wl.kappa, wl.rho]]), seed_noise
+
+
+def run_reconstruction(n=128, nt=40, precisions=("mixed", "fp64"), every=10):
+    from . import _abi
+    from . import synthetic as syn
+    from .context import Context
+    from .native import load
+
+    wl, tissue, centers, x_true, seed_noise = reconstruction_problem(n, nt)
+    api = load()
+    out = {"n": n, "nt": nt, "np": 216, "x_true_active": int(np.count_nonzero(x_true[:216]))}
+    data = None
+    for name in precisions:
+        prec = _abi.GLIA_MIXED if name == "mixed" else _abi.GLIA_FP64
+        ctx = Context(api, n, prec)
+        syn.setup_context(ctx, wl, tissue, centers, _abi.GLIA_HISTORY_CHECKPOINT, every)
+        ctx.set_obs_filter(np.ones(n ** 3))
+        if data is None:  # data from the FP64 forward at the true parameters
+            gen = Context(api, n, _abi.GLIA_FP64)
+            syn.setup_context(gen, wl, tissue, centers, _abi.GLIA_HISTORY_FULL, 0)
+            gen.set_coefficients(k=wl.kappa, rho=wl.rho, k_gm_wm=wl.k_gm_wm)
+            c1 = gen.solve_state(gen.phi_apply(x_true[:216]))
+            data = c1 + np.random.default_rng(seed_noise).normal(0.0, 0.01, c1.size)
+            gen.close()
+        lb, ub = reference_bounds(216)
+        x0 = np.concatenate([np.zeros(216), [0.5 * wl.kappa, 0.5 * wl.rho]])
+        t0 = time.perf_counter()
+        res = invert(ctx, data, x0, lb, ub)
+        wall = time.perf_counter() - t0
+        err_p = float(np.linalg.norm(res.x[:216] - x_true[:216]) / np.linalg.norm(x_true[:216]))
+        out[name] = {"wall_s": wall, "iterations": res.iterations, "fevals": res.fevals,
+                     "reason": res.reason, "J": res.J, "gnorm_rel": res.gnorm / res.gnorm0,
+                     "p_rel_err": err_p,
+                     "kappa": float(res.x[216]), "kappa_rel_err": abs(res.x[216] / x_true[216] - 1),
+                     "rho": float(res.x[217]), "rho_rel_err": abs(res.x[217] / x_true[217] - 1)}
+        ctx.close()
+    return out
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--nt", type=int, default=40)
+    ap.add_argument("--precisions", default="mixed,fp64")
+    a = ap.parse_args()
+    print(json.dumps(run_reconstruction(a.n, a.nt, tuple(a.precisions.split(",")))))
