@@ -93,6 +93,7 @@ SIGNATURES = {
     "set_pointer_mode": (c_int, [_CTX, c_int]),
     "set_stream": (c_int, [_CTX, c_void_p]),
     "synchronize": (c_int, [_CTX]),
+    "set_launch_geometry": (c_int, [_CTX, c_int, c_int]),
     "device_bytes": (c_int, [_CTX, POINTER(c_int64)]),
     "set_time": (c_int, [_CTX, c_double, c_int, c_int]),
     "set_pcg": (c_int, [_CTX, c_double, c_int, c_int, c_double]),

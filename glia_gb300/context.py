@@ -304,6 +304,13 @@ class Context:
     def reset_stats(self):
         self._call("reset_stats", self.api.reset_stats)
 
+    def set_launch_geometry(self, pointwise_blocks_per_sm: int, reduce_blocks_per_sm: int):
+        self._call("set_launch_geometry", self.api.set_launch_geometry,
+                   int(pointwise_blocks_per_sm), int(reduce_blocks_per_sm))
+
+    def set_stream(self, stream_handle: int):
+        self._call("set_stream", self.api.set_stream, ctypes.c_void_p(int(stream_handle)))
+
     def set_timing(self, enable: bool):
         self._call("set_timing", self.api.set_timing, int(enable))
 

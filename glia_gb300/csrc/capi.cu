@@ -91,6 +91,12 @@ int glia_set_pointer_mode(glia_ctx* ctx, int mode) {
 int glia_set_stream(glia_ctx* ctx, void* s) {
   return guarded(ctx, [&](glia::EngineBase& e) { e.set_stream(s); });
 }
+int glia_set_launch_geometry(glia_ctx* ctx, int pointwise_blocks_per_sm,
+                             int reduce_blocks_per_sm) {
+  return guarded(ctx, [&](glia::EngineBase& e) {
+    e.set_launch_geometry(pointwise_blocks_per_sm, reduce_blocks_per_sm);
+  });
+}
 int glia_synchronize(glia_ctx* ctx) {
   return guarded(ctx, [&](glia::EngineBase& e) { e.synchronize(); });
 }

@@ -14,6 +14,7 @@ class EngineBase {
   virtual void set_pointer_mode(int mode) = 0;
   virtual void set_stream(void* s) = 0;
   virtual void synchronize() = 0;
+  virtual void set_launch_geometry(int pw_per_sm, int red_per_sm) = 0;
   virtual int64_t device_bytes() const = 0;
   virtual void set_time(double dt, int nt, int order) = 0;
   virtual void set_pcg(double rtol, int maxit, int pc_dt_mode, double pc_dt) = 0;

@@ -90,6 +90,8 @@ struct SolveStatus {
   double dp;
 };
 
+constexpr int kMaxRedBlocksPerSm = 8;
+
 template <typename R>
 class Engine final : public EngineBase {
  public:
@@ -107,7 +109,7 @@ class Engine final : public EngineBase {
     GLIA_CUDA(cudaMemsetAsync(sc_, 0, sizeof(DevScalars), stream_));
     GLIA_CUDA(cudaMallocHost(&hsc_, sizeof(DevScalars)));
     GLIA_CUDA(cudaMallocHost(&hst_, sizeof(SolveStatus)));
-    ws_.partials = dalloc<double>((int64_t)red_blocks_ * 4);
+    ws_.partials = dalloc<double>((int64_t)sms_ * kMaxRedBlocksPerSm * 4);
     ws_.counter = dalloc<unsigned int>(1);
     GLIA_CUDA(cudaMemsetAsync(ws_.counter, 0, sizeof(unsigned int), stream_));
     for (R** f : {&wm_, &gm_, &csf_, &vt_, &bg_, &filter_, &kxx_, &rho_, &obs_, &c0_, &ct_, &p0_,
@@ -163,6 +165,18 @@ class Engine final : public EngineBase {
     if (zpass_) GLIA_CUFFT(cufftSetStream(p2d_, stream_));
   }
   void synchronize() override { GLIA_CUDA(cudaStreamSynchronize(stream_)); }
+  // CTAs per SM of the bandwidth kernels (grid-stride) and of the reducing kernels. Fewer CTAs
+  // let kernels of contexts on other streams run beside this one's (small grids, batches).
+  void set_launch_geometry(int pw_per_sm, int red_per_sm) override {
+    if (pw_per_sm < 1 || pw_per_sm > 16 || red_per_sm < 1 || red_per_sm > kMaxRedBlocksPerSm)
+      throw Error(GLIA_ERR_INVALID, "launch geometry: 1 <= pointwise <= 16, 1 <= reduce <= 8");
+    GLIA_CUDA(cudaStreamSynchronize(stream_));
+    pw_blocks_ = sms_ * pw_per_sm;
+    red_blocks_ = sms_ * red_per_sm;
+    if (cg_exec_) cudaGraphExecDestroy(cg_exec_);  // the PCG graph bakes the launch shapes in
+    cg_exec_ = nullptr;
+    if (graph_state_ > 0) graph_state_ = 0;
+  }
   int64_t device_bytes() const override { return bytes_; }
 
   void set_time(double dt, int nt, int order) override {

@@ -108,6 +108,11 @@ const char* glia_version(void);
 int glia_set_pointer_mode(glia_ctx* ctx, int mode);
 int glia_set_stream(glia_ctx* ctx, void* cuda_stream); /* NULL = the context's own stream */
 int glia_synchronize(glia_ctx* ctx);
+/* Launch shape (extension; no counterpart in the reference): CTAs per SM of the bandwidth
+ * kernels (1..16, default 8) and of the reducing kernels (1..8, default 4). Smaller grids let
+ * several contexts on different streams share the GPU (batches of small problems). */
+int glia_set_launch_geometry(glia_ctx* ctx, int pointwise_blocks_per_sm,
+                             int reduce_blocks_per_sm);
 /* Device bytes currently held by the context (fields, spectra, history, plans). */
 int glia_device_bytes(const glia_ctx* ctx, int64_t* bytes);
 
