@@ -139,10 +139,19 @@ def reference_bounds(np_: int, k_lb=1e-3, k_ub=1.0, rho_lb=1.0, rho_ub=15.0):
     return lb, ub
 
 
-def invert(ctx, d1, x0, lb, ub, settings: LbfgsSettings = LbfgsSettings()) -> LbfgsResult:
-    """L-BFGS on a configured context (objective = DerivativeOperatorsRD with all_gradients)."""
-    return bounded_lbfgs(lambda x: ctx.eval_objective_and_gradient(x, d1),
-                         lambda x: ctx.eval_objective(x, d1), x0, lb, ub, settings)
+def invert(ctx, d1, x0, lb, ub, settings: LbfgsSettings = LbfgsSettings(),
+           grad_scale=None) -> LbfgsResult:
+    """L-BFGS on a configured context (objective = DerivativeOperatorsRD with all_gradients).
+    grad_scale: the k_scale / rho_scale factors of x. The reference's adjoint gradient is taken
+    with respect to kappa and rho themselves, so the gradient with respect to the scaled unknowns
+    is that gradient times the scale (chain rule)."""
+    gs = 1.0 if grad_scale is None else np.asarray(grad_scale, dtype=np.float64)
+
+    def fg(x):
+        J, g = ctx.eval_objective_and_gradient(x, d1)
+        return J, g * gs
+
+    return bounded_lbfgs(fg, lambda x: ctx.eval_objective(x, d1), x0, lb, ub, settings)
 
 
 # ------------------------------------------------------------------------------------------
@@ -165,39 +174,65 @@ def reconstruction_problem(n=128, nt=40, seed_truth=4, seed_noise=5):
     return wl, tissue, centers, np.concatenate([p, [wl.kappa, wl.rho]]), seed_noise
 
 
-def run_reconstruction(n=128, nt=40, precisions=("mixed", "fp64"), every=10):
+def reconstruction_256(n=256, nt=100, n_gauss=1000, seed_truth=6):
+    """The 256^3 reconstruction: 1000 Gaussians (sigma = 2pi/64) at the first in-brain lattice
+    points, truth with 5 active, rho = 10, kappa = 0.05, dt = 0.01, nt = 100."""
+    from . import synthetic as syn
+
+    tissue = syn.make_tissue(n, 0)
+    centers = syn.lattice_centers_in_mask(tissue.mask, n_gauss)
+    rng = np.random.default_rng(seed_truth)
+    p = np.zeros(n_gauss)
+    act = rng.choice(n_gauss, size=5, replace=False)
+    p[act] = rng.uniform(0.5, 1.0, size=5)
+    wl = syn.GradientWorkload(n=n, nt=nt, n_gauss=n_gauss, rho=10.0, kappa=0.05)
+    return wl, tissue, centers, np.concatenate([p, [wl.kappa, wl.rho]]), 7
+
+
+def run_reconstruction(n=128, nt=40, precisions=("mixed", "fp64"), every=10, maxit=100,
+                       problem=None):
+    """L-BFGS from p = 0, kappa and rho at half their true values, to a 1e-3 relative reduction
+    of the projected gradient. kappa and rho enter x through the reference's k_scale_ /
+    rho_scale_ (x_kappa = kappa / 0.01, x_rho = rho / 10) so that all unknowns are O(1)."""
     from . import _abi
     from . import synthetic as syn
     from .context import Context
     from .native import load
 
-    wl, tissue, centers, x_true, seed_noise = reconstruction_problem(n, nt)
+    wl, tissue, centers, x_true, seed_noise = problem or reconstruction_problem(n, nt)
+    npp = len(centers)
+    k_scale, rho_scale = 1e-2, 10.0
+    scale = np.concatenate([np.ones(npp), [k_scale, rho_scale]])
     api = load()
-    out = {"n": n, "nt": nt, "np": 216, "x_true_active": int(np.count_nonzero(x_true[:216]))}
+    out = {"n": wl.n, "nt": wl.nt, "np": npp, "x_true_active": int(np.count_nonzero(x_true[:npp])),
+           "k_scale": k_scale, "rho_scale": rho_scale}
     data = None
     for name in precisions:
         prec = _abi.GLIA_MIXED if name == "mixed" else _abi.GLIA_FP64
-        ctx = Context(api, n, prec)
+        ctx = Context(api, wl.n, prec)
         syn.setup_context(ctx, wl, tissue, centers, _abi.GLIA_HISTORY_CHECKPOINT, every)
-        ctx.set_obs_filter(np.ones(n ** 3))
+        ctx.set_opt(k_scale=k_scale, rho_scale=rho_scale)
+        ctx.set_obs_filter(np.ones(wl.n ** 3))
         if data is None:  # data from the FP64 forward at the true parameters
-            gen = Context(api, n, _abi.GLIA_FP64)
+            gen = Context(api, wl.n, _abi.GLIA_FP64)
             syn.setup_context(gen, wl, tissue, centers, _abi.GLIA_HISTORY_FULL, 0)
             gen.set_coefficients(k=wl.kappa, rho=wl.rho, k_gm_wm=wl.k_gm_wm)
-            c1 = gen.solve_state(gen.phi_apply(x_true[:216]))
+            c1 = gen.solve_state(gen.phi_apply(x_true[:npp]))
             data = c1 + np.random.default_rng(seed_noise).normal(0.0, 0.01, c1.size)
             gen.close()
-        lb, ub = reference_bounds(216)
-        x0 = np.concatenate([np.zeros(216), [0.5 * wl.kappa, 0.5 * wl.rho]])
+        lb, ub = reference_bounds(npp)
+        lb, ub = lb / scale, ub / scale
+        x0 = np.concatenate([np.zeros(npp), [0.5 * wl.kappa, 0.5 * wl.rho]]) / scale
         t0 = time.perf_counter()
-        res = invert(ctx, data, x0, lb, ub)
+        res = invert(ctx, data, x0, lb, ub, LbfgsSettings(maxit=maxit), grad_scale=scale)
         wall = time.perf_counter() - t0
-        err_p = float(np.linalg.norm(res.x[:216] - x_true[:216]) / np.linalg.norm(x_true[:216]))
+        x = res.x * scale
+        err_p = float(np.linalg.norm(x[:npp] - x_true[:npp]) / np.linalg.norm(x_true[:npp]))
         out[name] = {"wall_s": wall, "iterations": res.iterations, "fevals": res.fevals,
-                     "reason": res.reason, "J": res.J, "gnorm_rel": res.gnorm / res.gnorm0,
-                     "p_rel_err": err_p,
-                     "kappa": float(res.x[216]), "kappa_rel_err": abs(res.x[216] / x_true[216] - 1),
-                     "rho": float(res.x[217]), "rho_rel_err": abs(res.x[217] / x_true[217] - 1)}
+                     "gevals": res.gevals, "reason": res.reason, "J": res.J,
+                     "gnorm_rel": res.gnorm / res.gnorm0, "p_rel_err": err_p,
+                     "kappa": float(x[npp]), "kappa_rel_err": abs(x[npp] / x_true[npp] - 1),
+                     "rho": float(x[npp + 1]), "rho_rel_err": abs(x[npp + 1] / x_true[npp + 1] - 1)}
         ctx.close()
     return out
 
@@ -207,5 +242,10 @@ if __name__ == "__main__":
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--nt", type=int, default=40)
     ap.add_argument("--precisions", default="mixed,fp64")
+    ap.add_argument("--maxit", type=int, default=100)
+    ap.add_argument("--full256", action="store_true",
+                    help="the 256^3 reconstruction with 1000 Gaussians (nt = 100)")
     a = ap.parse_args()
-    print(json.dumps(run_reconstruction(a.n, a.nt, tuple(a.precisions.split(",")))))
+    prob = reconstruction_256() if a.full256 else None
+    print(json.dumps(run_reconstruction(a.n, a.nt, tuple(a.precisions.split(",")),
+                                        maxit=a.maxit, problem=prob)))
