@@ -103,7 +103,9 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def dist_init(args):
+def dist_init(args=None, backend=None):
+    """One process per GPU (torchrun env). Ranks run independent problems; the process group
+    carries only the barrier and the max-over-ranks timing (nccl on GPUs, gloo on CPUs)."""
     import torch
 
     ws = int(os.environ.get("WORLD_SIZE", "1"))
@@ -112,8 +114,11 @@ def dist_init(args):
     if ws > 1:
         import torch.distributed as dist
 
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if backend is None:
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
     elif torch.cuda.is_available():
         torch.cuda.set_device(0)
     return ws, rank, local
@@ -132,7 +137,8 @@ def max_over_ranks(ws, v):
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -249,7 +255,8 @@ def main():
 
     ws, rank, local = dist_init(args)
     api = native.load()
-    wl, tissue, centers = build_workload(args, seed_offset=0)
+    # weak scaling: every rank solves its own problem (tissue seed = rank)
+    wl, tissue, centers = build_workload(args, seed_offset=rank)
     stream = torch.cuda.Stream()  # the library and the timing events share this stream
     with torch.cuda.stream(stream):
         run_ours(args, torch, api, wl, tissue, centers, stream, ws, rank)
