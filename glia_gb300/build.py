@@ -74,8 +74,7 @@ def build_callback_fatbin(cc=None) -> str | None:
     plan creation. Without it the library uses the separate k-multiply kernel."""
     cc = cc or nvcc()
     out = os.path.join(OUT_DIR, "cufft_cb.fatbin")
-    cmd = [cc, "-gencode", "arch=compute_103a,code=lto_103a",
-           "-gencode", "arch=compute_100,code=lto_100", "-dc", "-fatbin", "-O3",
+    cmd = [cc, "-gencode", "arch=compute_103a,code=lto_103a", "-dc", "-fatbin", "-O3",
            os.path.join(CSRC, "cufft_cb.cu"), "-o", out + ".tmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -18,7 +18,6 @@
 #include <dlfcn.h>
 
 #include <cufftXt.h>
-#include <cstdio>
 #include <fstream>
 #include <iterator>
 #include <string>
@@ -1384,51 +1383,26 @@ class Engine final : public EngineBase {
     if constexpr (std::is_same<R, float>::value) {
       const char* env = std::getenv("GLIA_CUFFT_CALLBACK");
       if (env && env[0] == '0') return;
-      const char* verbose = std::getenv("GLIA_VERBOSE");
-      auto note = [&](const char* stage, int code) {
-        if (verbose && verbose[0] == '1')
-          std::fprintf(stderr, "glia: cuFFT k-multiply callback unavailable (%s, code %d)\n",
-                       stage, code);
-      };
-      const std::string path = glia_library_dir() + "/cufft_cb.fatbin";
-      std::ifstream f(path, std::ios::binary);
-      if (!f) {
-        note(path.c_str(), -1);
-        return;
-      }
+      std::ifstream f(glia_library_dir() + "/cufft_cb.fatbin", std::ios::binary);
+      if (!f) return;
       std::vector<char> fatbin((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
       if (fatbin.empty()) return;
       GliaCbInfo hinfo{kxx_, (unsigned long long)N_};
       cbinfo_ = dalloc<GliaCbInfo>(1);
       GLIA_CUDA(cudaMemcpy(cbinfo_, &hinfo, sizeof(hinfo), cudaMemcpyHostToDevice));
       cufftHandle p = 0;
-      cufftResult r = cufftCreate(&p);
-      const char* stage = "cufftCreate";
-      if (r == CUFFT_SUCCESS) {
-        stage = "cufftSetAutoAllocation";
-        r = cufftSetAutoAllocation(p, 0);
-      }
+      bool ok = cufftCreate(&p) == CUFFT_SUCCESS;
+      ok = ok && cufftSetAutoAllocation(p, 0) == CUFFT_SUCCESS;
       void* info = cbinfo_;
-      if (r == CUFFT_SUCCESS) {
-        stage = "cufftXtSetJITCallback";
-        r = cufftXtSetJITCallback(p, "glia_store_times_k", fatbin.data(), fatbin.size(),
-                                  CUFFT_CB_ST_REAL, &info);
-      }
+      ok = ok && cufftXtSetJITCallback(p, "glia_store_times_k", fatbin.data(), fatbin.size(),
+                                       CUFFT_CB_ST_REAL, &info) == CUFFT_SUCCESS;
       int dims[3] = {g_.n, g_.n, g_.n};
-      if (r == CUFFT_SUCCESS) {
-        stage = "cufftMakePlanMany";
-        r = cufftMakePlanMany(p, 3, dims, nullptr, 1, (int)Ns_, nullptr, 1, (int)N_, CUFFT_C2R, 3,
-                              ws);
-      }
-      if (r == CUFFT_SUCCESS) {
-        stage = "cufftSetStream";
-        r = cufftSetStream(p, stream_);
-      }
-      if (r != CUFFT_SUCCESS) {
-        note(stage, (int)r);
+      ok = ok && cufftMakePlanMany(p, 3, dims, nullptr, 1, (int)Ns_, nullptr, 1, (int)N_,
+                                   CUFFT_C2R, 3, ws) == CUFFT_SUCCESS;
+      ok = ok && cufftSetStream(p, stream_) == CUFFT_SUCCESS;
+      if (!ok) {
         if (p) cufftDestroy(p);
         *ws = 0;
-        cudaGetLastError();
         return;
       }
       c2r3cb_ = p;
