@@ -220,20 +220,16 @@ def test_fused_zpass_against_oracle(n, monkeypatch):
 
 
 @pytest.mark.parametrize("n", [32, 64])
-def test_cufft_store_callback_matches_kernel_pass(n, monkeypatch):
-    """The k multiply as a cuFFT store callback against the separate k_mul_k3 pass."""
+def test_cufft_store_callback_is_bit_identical(n, monkeypatch):
+    """The k multiply as a cuFFT store callback gives the same bits as the k_mul_k3 pass."""
     wl, tissue, centers = small_problem(n, 3, n_gauss=8)
     d1 = observation(wl, tissue, centers)
     x = np.concatenate([np.linspace(0.1, 0.9, len(centers)), [wl.kappa, wl.rho]])
-    out, mul_launches = [], []
+    out = []
     for cb in ("1", "0"):
         monkeypatch.setenv("GLIA_CUFFT_CALLBACK", cb)
         g = gpu(n, MIXED)
         configure(g, wl, tissue, centers)
         g.set_obs_filter(np.ones(n ** 3))
-        g.set_timing(True)
         out.append(g.eval_objective_and_gradient(x, d1))
-        mul_launches.append(g.timing()["k_mul_k3"][0])
-    assert mul_launches[0] == 0 and mul_launches[1] > 0  # the callback replaced the pass
-    assert abs(out[0][0] - out[1][0]) <= 1e-6 * abs(out[1][0])
-    assert rel_l2(out[0][1], out[1][1]) < 1e-5
+    assert out[0][0] == out[1][0] and np.array_equal(out[0][1], out[1][1])
