@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libglia_rd.so")
-UNITS = ["capi.cu", "engine_f32.cu", "engine_f64.cu", "noalloc.cu"]  # cufft_cb.cu: separate fatbin
+UNITS = ["capi.cu", "engine_f32.cu", "engine_f64.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 
@@ -36,8 +36,6 @@ def up_to_date() -> bool:
     if not os.path.exists(LIB):
         return False
     t = os.path.getmtime(LIB)
-    if not os.path.exists(os.path.join(OUT_DIR, "cufft_cb.fatbin")):
-        return False
     return all(os.path.getmtime(s) <= t for s in _sources())
 
 
@@ -60,28 +58,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(compile_unit, UNITS))
     tmp = LIB + ".tmp"
-    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcufft", "-ldl"]
+    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcufft"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
-    build_callback_fatbin(cc)
     return LIB
-
-
-def build_callback_fatbin(cc=None) -> str | None:
-    """LTO-IR fatbin of the cuFFT store callback (csrc/cufft_cb.cu), loaded by the library at
-    plan creation. Without it the library uses the separate k-multiply kernel."""
-    cc = cc or nvcc()
-    out = os.path.join(OUT_DIR, "cufft_cb.fatbin")
-    cmd = [cc, "-gencode", "arch=compute_103a,code=lto_103a", "-dc", "-fatbin", "-O3",
-           os.path.join(CSRC, "cufft_cb.cu"), "-o", out + ".tmp"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        sys.stderr.write(f"cuFFT callback fatbin not built (k-multiply kernel used):\n{r.stderr}")
-        return None
-    os.replace(out + ".tmp", out)
-    return out
 
 
 if __name__ == "__main__":

@@ -15,12 +15,6 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
-#include <dlfcn.h>
-
-#include <cufftXt.h>
-#include <fstream>
-#include <iterator>
-#include <string>
 #include <cstring>
 #include <type_traits>
 #include <unordered_map>
@@ -98,23 +92,6 @@ struct SolveStatus {
 
 constexpr int kMaxRedBlocksPerSm = 8;
 
-// caller info of the cuFFT store callback in cufft_cb.cu (same layout)
-struct GliaCbInfo {
-  const float* k;
-  unsigned long long n3;
-};
-
-// Directory of the shared library that holds this code (where the build puts cufft_cb.fatbin).
-inline std::string glia_library_dir() {
-  Dl_info info;
-  if (dladdr(reinterpret_cast<void*>(&glia_library_dir), &info) && info.dli_fname) {
-    std::string p(info.dli_fname);
-    const size_t s = p.find_last_of('/');
-    return s == std::string::npos ? std::string(".") : p.substr(0, s);
-  }
-  return ".";
-}
-
 template <typename R>
 class Engine final : public EngineBase {
  public:
@@ -165,7 +142,7 @@ class Engine final : public EngineBase {
   ~Engine() override {
     cudaStreamSynchronize(stream_);
     if (cg_exec_) cudaGraphExecDestroy(cg_exec_);
-    for (cufftHandle* p : {&r2c1_, &c2r1_, &r2c3_, &c2r3_, &p2d_, &c2r3cb_})
+    for (cufftHandle* p : {&r2c1_, &c2r1_, &r2c3_, &c2r3_, &p2d_})
       if (*p) cufftDestroy(*p);
     destroy_batch_plans();
     for (auto& kv : sizes_) cudaFree(kv.first);
@@ -186,7 +163,6 @@ class Engine final : public EngineBase {
     stream_ = s ? (cudaStream_t)s : own_stream_;
     for (cufftHandle p : {r2c1_, c2r1_, r2c3_, c2r3_}) GLIA_CUFFT(cufftSetStream(p, stream_));
     if (zpass_) GLIA_CUFFT(cufftSetStream(p2d_, stream_));
-    if (c2r3cb_) GLIA_CUFFT(cufftSetStream(c2r3cb_, stream_));
   }
   void synchronize() override { GLIA_CUDA(cudaStreamSynchronize(stream_)); }
   // CTAs per SM of the bandwidth kernels (grid-stride) and of the reducing kernels. Fewer CTAs
@@ -431,7 +407,6 @@ class Engine final : public EngineBase {
       GLIA_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
       for (cufftHandle p : {r2c3_, c2r3_}) GLIA_CUFFT(cufftSetStream(p, cs));
       if (zpass_) GLIA_CUFFT(cufftSetStream(p2d_, cs));
-      if (c2r3cb_) GLIA_CUFFT(cufftSetStream(c2r3cb_, cs));
       stream_ = cs;
       GLIA_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
                                               cudaStreamCaptureModeThreadLocal));
@@ -456,7 +431,6 @@ class Engine final : public EngineBase {
     stream_ = saved;
     for (cufftHandle p : {r2c3_, c2r3_}) cufftSetStream(p, stream_);
     if (zpass_) cufftSetStream(p2d_, stream_);
-    if (c2r3cb_) cufftSetStream(c2r3cb_, stream_);
     if (cs) cudaStreamDestroy(cs);
     if (g) cudaGraphDestroy(g);
   }
@@ -490,15 +464,9 @@ class Engine final : public EngineBase {
                                                                             sc_));
   }
   // gradient spectra (g3s_) -> real gradient -> times k -> spectra of k * grad (g3s_).
-  // FP32: the k multiply runs as a store callback inside the batched C2R (cufft_cb.cu) when
-  // cuFFT could JIT-link it; otherwise the 3-D transforms sit around k_mul_k3. (The fused z pass,
-  // opt-in, replaces both.)
+  // FP32 with n = 64 ... 512: cuFFT does the (x, y) passes in place and k_zpass_mulk the fused
+  // z pass; otherwise three-dimensional cuFFT transforms around k_mul_k3.
   void apply_k_spectral() {
-    if (c2r3cb_) {
-      c2r(c2r3cb_, g3s_, g3r_, 3);
-      r2c(r2c3_, g3r_, g3s_, 3);
-      return;
-    }
     if (zpass_) {
       for (int j = 0; j < 3; j++) c2c2d(g3s_ + j * 2 * Ns_, CUFFT_INVERSE);
       const int lines = g_.n * g_.n;
@@ -1369,44 +1337,10 @@ class Engine final : public EngineBase {
                                 stream_));
       GLIA_CUDA(cudaStreamSynchronize(stream_));
     }
-    size_t wcb = 0;
-    if (!zpass_ && !ref_) make_callback_plan(&wcb);
-    fft_ws_bytes_ = std::max({w[0], w[1], w[2], w[3], w[4], wcb, (size_t)16});
+    fft_ws_bytes_ = std::max({w[0], w[1], w[2], w[3], w[4], (size_t)16});
     fft_ws_ = dalloc<char>((int64_t)fft_ws_bytes_);
     for (cufftHandle p : {r2c1_, c2r1_, r2c3_, c2r3_}) GLIA_CUFFT(cufftSetWorkArea(p, fft_ws_));
     if (zpass_) GLIA_CUFFT(cufftSetWorkArea(p2d_, fft_ws_));
-    if (c2r3cb_) GLIA_CUFFT(cufftSetWorkArea(c2r3cb_, fft_ws_));
-  }
-  // Batched C2R whose store callback multiplies by k (FP32 only). Any failure (no fatbin, no
-  // JIT-link support) leaves c2r3cb_ = 0 and the k_mul_k3 path in use.
-  void make_callback_plan(size_t* ws) {
-    if constexpr (std::is_same<R, float>::value) {
-      const char* env = std::getenv("GLIA_CUFFT_CALLBACK");
-      if (env && env[0] == '0') return;
-      std::ifstream f(glia_library_dir() + "/cufft_cb.fatbin", std::ios::binary);
-      if (!f) return;
-      std::vector<char> fatbin((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
-      if (fatbin.empty()) return;
-      GliaCbInfo hinfo{kxx_, (unsigned long long)N_};
-      cbinfo_ = dalloc<GliaCbInfo>(1);
-      GLIA_CUDA(cudaMemcpy(cbinfo_, &hinfo, sizeof(hinfo), cudaMemcpyHostToDevice));
-      cufftHandle p = 0;
-      bool ok = cufftCreate(&p) == CUFFT_SUCCESS;
-      ok = ok && cufftSetAutoAllocation(p, 0) == CUFFT_SUCCESS;
-      void* info = cbinfo_;
-      ok = ok && cufftXtSetJITCallback(p, "glia_store_times_k", fatbin.data(), fatbin.size(),
-                                       CUFFT_CB_ST_REAL, &info) == CUFFT_SUCCESS;
-      int dims[3] = {g_.n, g_.n, g_.n};
-      ok = ok && cufftMakePlanMany(p, 3, dims, nullptr, 1, (int)Ns_, nullptr, 1, (int)N_,
-                                   CUFFT_C2R, 3, ws) == CUFFT_SUCCESS;
-      ok = ok && cufftSetStream(p, stream_) == CUFFT_SUCCESS;
-      if (!ok) {
-        if (p) cufftDestroy(p);
-        *ws = 0;
-        return;
-      }
-      c2r3cb_ = p;
-    }
   }
   void c2c2d(R* data, int dir) {
     cudaEvent_t ev = tm_.begin(stream_);
@@ -1457,7 +1391,7 @@ class Engine final : public EngineBase {
     }
   }
   int fft_slot(cufftHandle p, bool fwd) const {
-    if (p == r2c3_ || p == c2r3_ || p == c2r3cb_) return fwd ? KS_FFT_R2C3 : KS_FFT_C2R3;
+    if (p == r2c3_ || p == c2r3_) return fwd ? KS_FFT_R2C3 : KS_FFT_C2R3;
     return fwd ? KS_FFT_R2C : KS_FFT_C2R;
   }
   void r2c(cufftHandle p, const R* in, R* out, int batch = 1) {
@@ -1468,9 +1402,7 @@ class Engine final : public EngineBase {
   void c2r(cufftHandle p, R* in, R* out, int batch = 1) {
     cudaEvent_t ev = tm_.begin(stream_);
     c2r_raw(p, in, out, batch);
-    // the callback plan also reads k once per voxel
-    tm_.end(fft_slot(p, false), ev, (double)batch * (FB() + SB()) + (p == c2r3cb_ ? FB() : 0.0),
-            stream_);
+    tm_.end(fft_slot(p, false), ev, (double)batch * (FB() + SB()), stream_);
   }
   void r2c_raw(cufftHandle p, const R* in, R* out, int batch) {
     if constexpr (std::is_same<R, float>::value)
@@ -1586,8 +1518,6 @@ class Engine final : public EngineBase {
 
   cufftHandle r2c1_ = 0, c2r1_ = 0, r2c3_ = 0, c2r3_ = 0, r2cB_ = 0, c2rB_ = 0, p2d_ = 0;
   bool zpass_ = false;   // fused z pass (FP32, n = 64 ... 512)
-  cufftHandle c2r3cb_ = 0;            // batched C2R with the k-multiply store callback
-  GliaCbInfo* cbinfo_ = nullptr;
   float2* tw_ = nullptr;
   char* fft_ws_ = nullptr;
   char* batch_ws_ = nullptr;

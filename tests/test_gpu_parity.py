@@ -217,19 +217,3 @@ def test_fused_zpass_against_oracle(n, monkeypatch):
     _, gro = o.eval_objective_and_gradient(x, d1)
     _, grg = g.eval_objective_and_gradient(x, d1)
     assert rel_l2(grg, gro) < GRAD_TOL
-
-
-@pytest.mark.parametrize("n", [32, 64])
-def test_cufft_store_callback_is_bit_identical(n, monkeypatch):
-    """The k multiply as a cuFFT store callback gives the same bits as the k_mul_k3 pass."""
-    wl, tissue, centers = small_problem(n, 3, n_gauss=8)
-    d1 = observation(wl, tissue, centers)
-    x = np.concatenate([np.linspace(0.1, 0.9, len(centers)), [wl.kappa, wl.rho]])
-    out = []
-    for cb in ("1", "0"):
-        monkeypatch.setenv("GLIA_CUFFT_CALLBACK", cb)
-        g = gpu(n, MIXED)
-        configure(g, wl, tissue, centers)
-        g.set_obs_filter(np.ones(n ** 3))
-        out.append(g.eval_objective_and_gradient(x, d1))
-    assert out[0][0] == out[1][0] and np.array_equal(out[0][1], out[1][1])
