@@ -943,10 +943,21 @@ class Engine final : public EngineBase {
       }
       if (!ref_ && trick) r2c(r2c1_, ct_, chat_hist_[nt_]);
     } else {
+      // the last segment is written straight into the segment buffers, so the backward sweep
+      // starts without recomputing it
+      const int S = (int)ckpt_.size(), last0 = (S - 1) * every_;
       for (int i = 0; i < nt_; i++) {
         if (i % every_ == 0) vcopy(ckpt_[i / every_], ct_);
-        step(ct_, nullptr, nullptr);
+        if (i >= last0) {
+          vcopy(seg_c_[i - last0], ct_);
+          step(ct_, trick ? seg_chat_[i - last0] : nullptr, seg_half_[i - last0]);
+        } else {
+          step(ct_, nullptr, nullptr);
+        }
       }
+      vcopy(seg_c_[nt_ - last0], ct_);
+      if (trick) r2c(r2c1_, ct_, seg_chat_[nt_ - last0]);
+      last_seg_resident_ = true;
     }
     sync_sweep();
     state_done_ = true;
@@ -1055,20 +1066,24 @@ class Engine final : public EngineBase {
       if (accumulate) grad_point(nt_, ct_, explicit_kappa);
       for (int s = S - 1; s >= 0; s--) {
         const int i0 = s * every_, i1 = std::min(nt_, (s + 1) * every_);
-        vcopy(seg_c_[0], ckpt_[s]);
-        vcopy(tmp2(), ckpt_[s]);
-        for (int i = i0; i < i1; i++) {
-          // recompute solves are neither state nor adjoint solves (which = 2)
-          step(tmp2(), trick ? seg_chat_[i - i0] : nullptr, seg_half_[i - i0], 2);
-          vcopy(seg_c_[i - i0 + 1], tmp2());
+        // the last segment is still resident from the forward sweep (first adjoint only)
+        if (s < S - 1 || !last_seg_resident_) {
+          vcopy(seg_c_[0], ckpt_[s]);
+          vcopy(tmp2(), ckpt_[s]);
+          for (int i = i0; i < i1; i++) {
+            // recompute solves are neither state nor adjoint solves (which = 2)
+            step(tmp2(), trick ? seg_chat_[i - i0] : nullptr, seg_half_[i - i0], 2);
+            vcopy(seg_c_[i - i0 + 1], tmp2());
+          }
+          if (trick) r2c(r2c1_, tmp2(), seg_chat_[i1 - i0]);
         }
-        if (trick) r2c(r2c1_, tmp2(), seg_chat_[i1 - i0]);
         for (int i = i1 - 1; i >= i0; i--) {
           adjoint_step(i, seg_half_[i - i0], trick ? seg_chat_[i - i0 + 1] : nullptr,
                        accumulate && trick);
           if (accumulate) grad_point(i, seg_c_[i - i0], explicit_kappa);
         }
         if (s == 0 && accumulate && trick) kappa_dot_at(seg_chat_[0], 0.5 * dt_);
+        last_seg_resident_ = false;  // the segment buffers now hold another segment
       }
     }
     sync_sweep();
@@ -1514,6 +1529,7 @@ class Engine final : public EngineBase {
   KTimer tm_;
   int graph_state_ = 0;  // 0 not built, 1 built, -1 unavailable (host-driven loop)
   bool graph_solves_ = false;  // the current sweep ran PCG loops as graphs
+  bool last_seg_resident_ = false;  // segment buffers hold the last segment of the forward
   cudaGraphExec_t cg_exec_ = nullptr;
 
   cufftHandle r2c1_ = 0, c2r1_ = 0, r2c3_ = 0, c2r3_ = 0, r2cB_ = 0, c2rB_ = 0, p2d_ = 0;

@@ -217,3 +217,20 @@ def test_fused_zpass_against_oracle(n, monkeypatch):
     _, gro = o.eval_objective_and_gradient(x, d1)
     _, grg = g.eval_objective_and_gradient(x, d1)
     assert rel_l2(grg, gro) < GRAD_TOL
+
+
+def test_repeated_adjoint_after_one_state_solve_checkpointed():
+    """Two adjoint sweeps after one state solve (checkpointed history) give the same result."""
+    n, nt = 32, 7
+    wl, tissue, centers = small_problem(n, nt)
+    g = gpu(n, MIXED)
+    configure(g, wl, tissue, centers, _abi.GLIA_HISTORY_CHECKPOINT, 3)
+    c1 = g.solve_state(g.phi_apply(np.linspace(0.2, 1.0, len(centers))))
+    pt = -(c1 - 0.5 * c1.max())
+    a = g.solve_adjoint(pt)
+    b = g.solve_adjoint(pt)
+    assert np.array_equal(a, b)
+    f = gpu(n, MIXED)
+    configure(f, wl, tissue, centers)
+    f.solve_state(f.phi_apply(np.linspace(0.2, 1.0, len(centers))))
+    assert rel_l2(a, f.solve_adjoint(pt)) < 1e-12
