@@ -24,6 +24,7 @@
 #include "kernels.cuh"
 #include "ktimer.cuh"
 #include "zpass.cuh"
+#include "xpass.cuh"
 
 #define GLIA_TIMED(slot, bytes, ...)             \
   do {                                           \
@@ -142,7 +143,7 @@ class Engine final : public EngineBase {
   ~Engine() override {
     cudaStreamSynchronize(stream_);
     if (cg_exec_) cudaGraphExecDestroy(cg_exec_);
-    for (cufftHandle* p : {&r2c1_, &c2r1_, &r2c3_, &c2r3_, &p2d_})
+    for (cufftHandle* p : {&r2c1_, &c2r1_, &r2c3_, &c2r3_, &p2d_, &r2c2d3_, &c2r2d3_})
       if (*p) cufftDestroy(*p);
     destroy_batch_plans();
     for (auto& kv : sizes_) cudaFree(kv.first);
@@ -163,6 +164,8 @@ class Engine final : public EngineBase {
     stream_ = s ? (cudaStream_t)s : own_stream_;
     for (cufftHandle p : {r2c1_, c2r1_, r2c3_, c2r3_}) GLIA_CUFFT(cufftSetStream(p, stream_));
     if (zpass_) GLIA_CUFFT(cufftSetStream(p2d_, stream_));
+    if (xpass_)
+      for (cufftHandle p : {r2c2d3_, c2r2d3_}) GLIA_CUFFT(cufftSetStream(p, stream_));
   }
   void synchronize() override { GLIA_CUDA(cudaStreamSynchronize(stream_)); }
   // CTAs per SM of the bandwidth kernels (grid-stride) and of the reducing kernels. Fewer CTAs
@@ -338,11 +341,8 @@ class Engine final : public EngineBase {
     GLIA_LAUNCH_CHECK();
     // set-up: chat = F c; D c; b = c + a D c; r0 = 2 a D c; x0 = c; n = 0 convergence test
     r2c(r2c1_, c, chat);
-    launch_grad3<false>(chat, nullptr);
-    apply_k_spectral();
-    GLIA_TIMED(KS_DIV_SETUP, SB() * (cx ? 7 : 6),
-               k_spec_div<R, EPI_SETUP><<<red_blocks_, kThreads, 0, stream_>>>(
-                   g_, g3s_, chat, cx, xhat_, rhat_, R(0), sc_, ws_));
+    d_front<false>(chat, nullptr);
+    d_back<EPI_SETUP>(chat, cx, xhat_, rhat_, R(0));
     if (use_graph()) {
       GLIA_CUDA(cudaGraphLaunch(cg_exec_, stream_));  // the whole PCG loop, no host round trip
       graph_solves_ = true;
@@ -358,13 +358,74 @@ class Engine final : public EngineBase {
     GLIA_LAUNCH_CHECK();
   }
 
+  // First half of a spectral D apply: the three spectra of k grad u in g3s_, from the spectrum
+  // src (plain) or from the new PCG direction p = P r + b p (CGDIR: src = r, pdir = p). With the
+  // x pass (FP32, n = 64 ... 256) the layout of g3s_ is (x, ky, kz) per component (the x
+  // transform is done by k_xinv / k_xfwd, cuFFT does batched 2-D (y, z) transforms); otherwise
+  // it is the full 3-D spectrum.
+  template <bool CGDIR>
+  void d_front(const R* src, R* pdir) {
+    if (xpass_) {
+      GLIA_TIMED(KS_XINV, SB() * (CGDIR ? 6 : 4), launch_xinv<CGDIR>(src, pdir));
+      c2r(c2r2d3_, g3s_, g3r_, 3);
+      GLIA_TIMED(KS_MUL_K3, FB() * 7,
+                 k_mul_k3<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, g3r_, kxx_, sc_, 0));
+      r2c(r2c2d3_, g3r_, g3s_, 3);
+      return;
+    }
+    launch_grad3<CGDIR>(src, pdir);
+    apply_k_spectral();
+  }
+  // Second half: divergence of k grad u in spectral space and the caller's epilogue
+  // (k_spec_div semantics: EPI_APPLYD out = scale D; EPI_SETUP solve set-up; EPI_CGW w = A p).
+  template <int EPI>
+  void d_back(const R* aux_in, const R* cx, R* out, R* aux_out, R scale) {
+    const double bytes = EPI == EPI_APPLYD ? SB() * 4
+                         : EPI == EPI_SETUP ? SB() * (cx ? 7 : 6)
+                                            : SB() * 5;
+    const int slot = EPI == EPI_APPLYD ? KS_DIV_APPLYD : (EPI == EPI_SETUP ? KS_DIV_SETUP : KS_DIV_CGW);
+    const int blocks = EPI == EPI_APPLYD ? pw_blocks_ : red_blocks_;
+    if (xpass_) {
+      GLIA_TIMED(slot, bytes, launch_xfwd<EPI>(aux_in, cx, out, aux_out, scale, blocks));
+      return;
+    }
+    GLIA_TIMED(slot, bytes,
+               k_spec_div<R, EPI><<<blocks, kThreads, 0, stream_>>>(g_, g3s_, aux_in, cx, out,
+                                                                    aux_out, scale, sc_, ws_));
+  }
+  template <bool CGDIR>
+  void launch_xinv(const R* src, R* pdir) {
+    if constexpr (std::is_same<R, float>::value) {
+      constexpr int MODE = CGDIR ? 1 : 0;
+      const int n = g_.n;
+      if (n == 256)
+        k_xinv<256, MODE><<<pw_blocks_, 256, 0, stream_>>>(g_, src, pdir, g3s_, sc_, tw256_);
+      else if (n == 128)
+        k_xinv<128, MODE><<<pw_blocks_, 256, 0, stream_>>>(g_, src, pdir, g3s_, sc_, tw256_);
+      else
+        k_xinv<64, MODE><<<pw_blocks_, 256, 0, stream_>>>(g_, src, pdir, g3s_, sc_, tw256_);
+    }
+  }
+  template <int EPI>
+  void launch_xfwd(const R* aux_in, const R* cx, R* out, R* aux_out, R scale, int blocks) {
+    if constexpr (std::is_same<R, float>::value) {
+      const int n = g_.n;
+      if (n == 256)
+        k_xfwd<256, EPI><<<blocks, 256, 0, stream_>>>(g_, g3s_, aux_in, cx, out, aux_out, scale,
+                                                      sc_, ws_, tw256_);
+      else if (n == 128)
+        k_xfwd<128, EPI><<<blocks, 256, 0, stream_>>>(g_, g3s_, aux_in, cx, out, aux_out, scale,
+                                                      sc_, ws_, tw256_);
+      else
+        k_xfwd<64, EPI><<<blocks, 256, 0, stream_>>>(g_, g3s_, aux_in, cx, out, aux_out, scale,
+                                                     sc_, ws_, tw256_);
+    }
+  }
+
   // one PCG iteration of the fused engine (launched directly, or captured as the loop body)
   void cg_iteration() {
-    launch_grad3<true>(rhat_, phat_);  // p = P r + b p, gradient spectra of p
-    apply_k_spectral();                // 3 C2R, k *, 3 R2C
-    GLIA_TIMED(KS_DIV_CGW, SB() * 5,
-               k_spec_div<R, EPI_CGW><<<red_blocks_, kThreads, 0, stream_>>>(
-                   g_, g3s_, phat_, nullptr, what_, nullptr, R(0), sc_, ws_));
+    d_front<true>(rhat_, phat_);  // p = P r + b p and the spectra of k grad p
+    d_back<EPI_CGW>(phat_, nullptr, what_, nullptr, R(0));  // w = A p, <p, w>, alpha
     GLIA_TIMED(KS_CG_UPDATE, SB() * 6,
                k_cg_update<R><<<red_blocks_, kThreads, 0, stream_>>>(g_, xhat_, phat_, rhat_,
                                                                      what_, sc_, ws_));
@@ -407,6 +468,8 @@ class Engine final : public EngineBase {
       GLIA_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
       for (cufftHandle p : {r2c3_, c2r3_}) GLIA_CUFFT(cufftSetStream(p, cs));
       if (zpass_) GLIA_CUFFT(cufftSetStream(p2d_, cs));
+      if (xpass_)
+        for (cufftHandle p : {r2c2d3_, c2r2d3_}) GLIA_CUFFT(cufftSetStream(p, cs));
       stream_ = cs;
       GLIA_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
                                               cudaStreamCaptureModeThreadLocal));
@@ -431,6 +494,8 @@ class Engine final : public EngineBase {
     stream_ = saved;
     for (cufftHandle p : {r2c3_, c2r3_}) cufftSetStream(p, stream_);
     if (zpass_) cufftSetStream(p2d_, stream_);
+    if (xpass_)
+      for (cufftHandle p : {r2c2d3_, c2r2d3_}) cufftSetStream(p, stream_);
     if (cs) cudaStreamDestroy(cs);
     if (g) cudaGraphDestroy(g);
   }
@@ -635,11 +700,8 @@ class Engine final : public EngineBase {
       return;
     }
     r2c(r2c1_, c, chat_);
-    launch_grad3<false>(chat_, nullptr);
-    apply_k_spectral();
-    k_spec_div<R, EPI_APPLYD><<<pw_blocks_, kThreads, 0, stream_>>>(
-        g_, g3s_, nullptr, nullptr, xhat_, nullptr, (R)g_.invN, sc_, ws_);
-    GLIA_LAUNCH_CHECK();
+    d_front<false>(chat_, nullptr);
+    d_back<EPI_APPLYD>(nullptr, nullptr, xhat_, nullptr, (R)g_.invN);
     c2r(c2r1_, xhat_, dc);
   }
   void apply_d(const void* c, void* dc) override {
@@ -1099,11 +1161,8 @@ class Engine final : public EngineBase {
     GLIA_LAUNCH_CHECK();
     R* spec_a = xhat_;
     r2c(r2c1_, p0_, spec_a);
-    launch_grad3<false>(spec_a, nullptr);
-    apply_k_spectral();
-    k_spec_div<R, EPI_SETUP><<<red_blocks_, kThreads, 0, stream_>>>(g_, g3s_, spec_a, chat0,
-                                                                     rhat_, what_, R(0), sc_, ws_);
-    GLIA_LAUNCH_CHECK();
+    d_front<false>(spec_a, nullptr);
+    d_back<EPI_SETUP>(spec_a, chat0, rhat_, what_, R(0));
   }
   void solve_adjoint(const void* pt, void* a0) override {
     if (pt) import_field(pt, pt_);
@@ -1352,10 +1411,38 @@ class Engine final : public EngineBase {
                                 stream_));
       GLIA_CUDA(cudaStreamSynchronize(stream_));
     }
-    fft_ws_bytes_ = std::max({w[0], w[1], w[2], w[3], w[4], (size_t)16});
+    // x pass fused into the spectral kernels: cuFFT does contiguous batched 2-D (y, z)
+    // transforms of the three gradient components (3n planes); default on (GLIA_XPASS=0 off)
+    const char* xoff = std::getenv("GLIA_XPASS");
+    xpass_ = std::is_same<R, float>::value && (n == 64 || n == 128 || n == 256) && !zpass_ &&
+             !ref_ && !(xoff && xoff[0] == '0');
+    size_t w2[2] = {0, 0};
+    if (xpass_) {
+      int dims[2] = {n, n};
+      for (int d = 0; d < 2; d++) {
+        cufftHandle& p = d == 0 ? r2c2d3_ : c2r2d3_;
+        GLIA_CUFFT(cufftCreate(&p));
+        GLIA_CUFFT(cufftSetAutoAllocation(p, 0));
+        const bool fwd = d == 0;
+        GLIA_CUFFT(cufftMakePlanMany(p, 2, dims, nullptr, 1, fwd ? n * n : n * g_.nh, nullptr, 1,
+                                     fwd ? n * g_.nh : n * n, fwd ? CT<R>::kR2C : CT<R>::kC2R,
+                                     3 * n, &w2[d]));
+        GLIA_CUFFT(cufftSetStream(p, stream_));
+      }
+      std::vector<float2> tw(256);
+      for (int j = 0; j < 256; j++) {
+        const double a = -2.0 * M_PI * (double)j / 256.0;
+        tw[j] = make_float2((float)std::cos(a), (float)std::sin(a));
+      }
+      tw256_ = dalloc<float2>(256);
+      GLIA_CUDA(cudaMemcpy(tw256_, tw.data(), 256 * sizeof(float2), cudaMemcpyHostToDevice));
+    }
+    fft_ws_bytes_ = std::max({w[0], w[1], w[2], w[3], w[4], w2[0], w2[1], (size_t)16});
     fft_ws_ = dalloc<char>((int64_t)fft_ws_bytes_);
     for (cufftHandle p : {r2c1_, c2r1_, r2c3_, c2r3_}) GLIA_CUFFT(cufftSetWorkArea(p, fft_ws_));
     if (zpass_) GLIA_CUFFT(cufftSetWorkArea(p2d_, fft_ws_));
+    if (xpass_)
+      for (cufftHandle p : {r2c2d3_, c2r2d3_}) GLIA_CUFFT(cufftSetWorkArea(p, fft_ws_));
   }
   void c2c2d(R* data, int dir) {
     cudaEvent_t ev = tm_.begin(stream_);
@@ -1406,7 +1493,8 @@ class Engine final : public EngineBase {
     }
   }
   int fft_slot(cufftHandle p, bool fwd) const {
-    if (p == r2c3_ || p == c2r3_) return fwd ? KS_FFT_R2C3 : KS_FFT_C2R3;
+    if (p == r2c3_ || p == c2r3_ || p == r2c2d3_ || p == c2r2d3_)
+      return fwd ? KS_FFT_R2C3 : KS_FFT_C2R3;
     return fwd ? KS_FFT_R2C : KS_FFT_C2R;
   }
   void r2c(cufftHandle p, const R* in, R* out, int batch = 1) {
@@ -1534,6 +1622,9 @@ class Engine final : public EngineBase {
 
   cufftHandle r2c1_ = 0, c2r1_ = 0, r2c3_ = 0, c2r3_ = 0, r2cB_ = 0, c2rB_ = 0, p2d_ = 0;
   bool zpass_ = false;   // fused z pass (FP32, n = 64 ... 512)
+  bool xpass_ = false;   // x pass fused into the spectral kernels (FP32, n = 64 ... 256)
+  cufftHandle r2c2d3_ = 0, c2r2d3_ = 0;  // batched 2-D (y, z) transforms, 3n planes
+  float2* tw256_ = nullptr;
   float2* tw_ = nullptr;
   char* fft_ws_ = nullptr;
   char* batch_ws_ = nullptr;

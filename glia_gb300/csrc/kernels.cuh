@@ -138,6 +138,44 @@ __global__ void __launch_bounds__(kThreads)
 
 enum DivEpi { EPI_APPLYD = 0, EPI_SETUP = 1, EPI_CGW = 2 };
 
+// Scalar epilogue of a solve set-up (last block, thread 0): PETSc's n = 0 convergence test from
+// sums = [||B b||^2, ||z0||^2, <z0, r0>, <cx, D c>] (Parseval sums, times 1/N).
+__device__ __forceinline__ void div_setup_finish(const double (&sums)[4], DevScalars* sc,
+                                                 double invN, bool has_cx) {
+  double dp = sqrt(sums[1] * invN), snorm = sqrt(sums[0] * invN);
+  if (snorm == 0.0) snorm = dp;
+  sc->rnorm0 = snorm;
+  sc->ttol = fmax(sc->rtol * snorm, sc->abstol);
+  sc->dp = dp;
+  sc->it = 0;
+  sc->iter = 0;
+  sc->dpi = 0.0;
+  sc->bcoef = 0.0;
+  sc->beta = sums[2] * invN;
+  int st = conv_test(dp, sc);
+  if (st == 0 && sc->beta == 0.0) {
+    st = 2;
+    sc->it = 1;
+  }
+  sc->status = st;
+  if (has_cx) sc->acc[6] += sc->kdot_weight * sums[3] * invN;
+}
+
+// Scalar epilogue of w = A p (last block, thread 0): PETSc's indefiniteness check, alpha.
+__device__ __forceinline__ void div_cgw_finish(double pw_sum, DevScalars* sc, double invN) {
+  const double dpi = pw_sum * invN;
+  sc->dpi_old = sc->dpi;
+  sc->dpi = dpi;
+  sc->beta_old = sc->beta;
+  sc->it = sc->iter + 1;
+  if (dpi == 0.0 || (sc->iter > 0 && dpi * sc->dpi_old <= 0.0))
+    sc->status = -8;
+  else if (isnan(dpi) || isinf(dpi))
+    sc->status = -9;
+  else
+    sc->alpha = sc->beta / dpi;
+}
+
 // Divergence in spectral space, D = sum_j i w_j G_j (the spectrum of div(k grad u)), fused with
 // the epilogue of its caller:
 //  EPI_APPLYD: out = scale * D.
@@ -208,42 +246,11 @@ __global__ void __launch_bounds__(kThreads)
   } else if constexpr (EPI == EPI_SETUP) {
     double sums[4] = {acc[0].value(), acc[1].value(), acc[2].value(), acc[3].value()};
     if (!grid_sum_last<4>(sums, ws)) return;
-    if (threadIdx.x == 0) {
-      const double invNd = g.invN;
-      double dp = sqrt(sums[1] * invNd), snorm = sqrt(sums[0] * invNd);
-      if (snorm == 0.0) snorm = dp;
-      sc->rnorm0 = snorm;
-      sc->ttol = fmax(sc->rtol * snorm, sc->abstol);
-      sc->dp = dp;
-      sc->it = 0;
-      sc->iter = 0;
-      sc->dpi = 0.0;
-      sc->bcoef = 0.0;
-      sc->beta = sums[2] * invNd;
-      int st = conv_test(dp, sc);
-      if (st == 0 && sc->beta == 0.0) {
-        st = 2;
-        sc->it = 1;
-      }
-      sc->status = st;
-      if (cx) sc->acc[6] += sc->kdot_weight * sums[3] * invNd;
-    }
+    if (threadIdx.x == 0) div_setup_finish(sums, sc, g.invN, cx != nullptr);
   } else {
     double a1[1] = {acc[0].value()};
     if (!grid_sum_last<1>(a1, ws)) return;
-    if (threadIdx.x == 0) {
-      const double dpi = a1[0] * g.invN;
-      sc->dpi_old = sc->dpi;
-      sc->dpi = dpi;
-      sc->beta_old = sc->beta;
-      sc->it = sc->iter + 1;
-      if (dpi == 0.0 || (sc->iter > 0 && dpi * sc->dpi_old <= 0.0))
-        sc->status = -8;
-      else if (isnan(dpi) || isinf(dpi))
-        sc->status = -9;
-      else
-        sc->alpha = sc->beta / dpi;
-    }
+    if (threadIdx.x == 0) div_cgw_finish(a1[0], sc, g.invN);
   }
 }
 

@@ -35,6 +35,7 @@ enum KSlot {
   KS_REF_DOT,            // reference-structured inner products
   KS_ZPASS,              // k_zpass_mulk: fused z C2R, k multiply, z R2C
   KS_FFT_2D,             // cuFFT 2-D C2C over (x, y) for every kz
+  KS_XINV,               // k_xinv: PCG direction, gradient spectra, inverse x transforms
   KS_COUNT
 };
 
@@ -44,7 +45,7 @@ static const char* const kSlotNames[KS_COUNT] = {
     "k_reaction_lin",     "k_grad_acc",     "k_obs_residual",  "k_phi",
     "copy_d2d",           "cufft_r2c",      "cufft_c2r",       "cufft_r2c_x3",
     "cufft_c2r_x3",       "ref_vector_ops", "ref_dot",         "k_zpass_mulk",
-    "cufft_c2c_2d"};
+    "cufft_c2c_2d",       "k_xinv"};
 
 struct KTimer {
   bool on = false;

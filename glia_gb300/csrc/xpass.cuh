@@ -1,0 +1,311 @@
+// xpass.cuh — the x direction of the spectral D apply, fused into the kernels that already stream
+// the spectra (FP32, n = 64, 128, 256).
+//
+// A three-dimensional transform is a 2-D transform over (y, z) for every x plus a 1-D transform
+// along x. cuFFT does the (y, z) part as a contiguous batched 2-D transform; these kernels do the
+// x part inside the passes around it:
+//  k_xinv: new PCG direction p = P r + b p (or a plain spectrum), the three gradient spectra
+//          i w_j p / N, and their inverse transforms along x -> G_j(x, ky, kz);
+//  k_xfwd: forward transforms along x of the three spectra of k grad p, the divergence
+//          sum_j i w_j F_j, and the epilogue of k_spec_div (CG operator / solve set-up / plain D).
+// Each CTA owns a tile: all n rows along x times T consecutive (ky, kz) columns of the flattened
+// (ky, kz) plane (T complex = 128 to 512 contiguous bytes per row). The n-point DFT along x is
+// R1 x R2: an R1-point DFT in registers over x = R2 a + b, a twiddle exp(s 2 pi i b k1 / n), one
+// exchange through shared memory, and an R2-point DFT in registers giving k = k1 + R1 k2.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace glia {
+
+template <int NN>
+struct XDecomp;
+template <>
+struct XDecomp<256> {
+  static constexpr int R1 = 16, R2 = 16, T = 16;
+};
+template <>
+struct XDecomp<128> {
+  static constexpr int R1 = 16, R2 = 8, T = 32;
+};
+template <>
+struct XDecomp<64> {
+  static constexpr int R1 = 8, R2 = 8, T = 64;
+};
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul2(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// exp(-2 pi i j / 16), j in [0, 16)
+__device__ __forceinline__ float2 w16(int j) {
+  constexpr float c[16] = {1.000000000f,  0.923879533f,  0.707106781f,  0.382683432f,
+                           0.000000000f,  -0.382683432f, -0.707106781f, -0.923879533f,
+                           -1.000000000f, -0.923879533f, -0.707106781f, -0.382683432f,
+                           0.000000000f,  0.382683432f,  0.707106781f,  0.923879533f};
+  constexpr float s[16] = {0.000000000f,  -0.382683432f, -0.707106781f, -0.923879533f,
+                           -1.000000000f, -0.923879533f, -0.707106781f, -0.382683432f,
+                           0.000000000f,  0.382683432f,  0.707106781f,  0.923879533f,
+                           1.000000000f,  0.923879533f,  0.707106781f,  0.382683432f};
+  return make_float2(c[j & 15], s[j & 15]);
+}
+
+__host__ __device__ constexpr int brev_bits(int i, int bits) {
+  int r = 0;
+  for (int b = 0; b < bits; b++)
+    if (i & (1 << b)) r |= 1 << (bits - 1 - b);
+  return r;
+}
+
+// In-register DFT of size R (8 or 16): X[k] = sum_i v[i] exp(S 2 pi i i k / R), natural order in
+// and out (iterative radix-2 on the bit-reversed copy).
+template <int R, int S>
+__device__ __forceinline__ void reg_dft(float2 (&v)[R]) {
+  constexpr int LOG = R == 16 ? 4 : 3;
+  float2 t[R];
+#pragma unroll
+  for (int i = 0; i < R; i++) t[brev_bits(i, LOG)] = v[i];
+#pragma unroll
+  for (int len = 2; len <= R; len <<= 1) {
+#pragma unroll
+    for (int i = 0; i < R; i += len) {
+#pragma unroll
+      for (int j = 0; j < len / 2; j++) {
+        float2 w = w16(j * (16 / len));
+        if (S > 0) w.y = -w.y;
+        const float2 u = t[i + j];
+        const float2 x = cmul2(t[i + j + len / 2], w);
+        t[i + j] = cadd(u, x);
+        t[i + j + len / 2] = csub(u, x);
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < R; i++) v[i] = t[i];
+}
+
+// twiddle exp(S 2 pi i e / n) from the shared table W_256^j = exp(-2 pi i j / 256)
+template <int NN, int S>
+__device__ __forceinline__ float2 tw_n(const float2* tw, int e) {
+  float2 w = tw[(e * (256 / NN)) & 255];
+  if (S > 0) w.y = -w.y;
+  return w;
+}
+
+// Column geometry of a tile: flattened (ky, kz) index q, its wave numbers and multiplicity.
+struct XCol {
+  int64_t q;
+  int wy, wz;
+  float mult;
+};
+__device__ __forceinline__ XCol xcol(const Geo& g, int64_t q) {
+  XCol c;
+  c.q = q;
+  const uint32_t ky = g.fd_nh.div((uint32_t)q);
+  const uint32_t kz = (uint32_t)q - ky * (uint32_t)g.nh;
+  c.wy = wavenum((int)ky, g.n);
+  c.wz = wavenum((int)kz, g.n);
+  c.mult = (kz == 0 || (int)kz == g.n / 2) ? 1.f : 2.f;
+  return c;
+}
+
+// MODE 0: spectrum src -> G; MODE 1: PCG direction p = P r + b p (r = src, p = pdir, p written).
+template <int NN, int MODE>
+__global__ void __launch_bounds__(256, 2)
+    k_xinv(Geo g, const float* __restrict__ src, float* __restrict__ pdir, float* __restrict__ G3,
+           const DevScalars* __restrict__ sc, const float2* __restrict__ tw_g) {
+  using D = XDecomp<NN>;
+  constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
+  constexpr int NB1 = R2 / GR, NB2 = R1 / GR;
+  __shared__ float2 sm[NN * T];
+  __shared__ float2 tw[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw_g[i];
+  __syncthreads();
+  if (MODE == 1 && sc->status != 0) return;
+  const int c = threadIdx.x % T, gi = threadIdx.x / T;
+  const int64_t plane = (int64_t)g.n * g.nh;
+  const int ntiles = (int)(plane / T);
+  const float invN = (float)g.invN;
+  const bool first = MODE == 1 ? sc->iter == 0 : true;
+  const float bc = MODE == 1 ? (float)sc->bcoef : 0.f;
+  const float pcc = MODE == 1 ? (float)sc->pc_c : 0.f;
+  const float2* S = reinterpret_cast<const float2*>(src);
+  float2* P = reinterpret_cast<float2*>(pdir);
+  float2* Gc = reinterpret_cast<float2*>(G3);
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const XCol col = xcol(g, (int64_t)tile * T + c);
+    float2 v[NB1][R1];
+#pragma unroll
+    for (int m = 0; m < NB1; m++) {
+      const int b = gi + GR * m;
+#pragma unroll
+      for (int a = 0; a < R1; a++) {
+        const int kx = R2 * a + b;
+        const int64_t idx = (int64_t)kx * plane + col.q;
+        float2 val = S[idx];
+        if (MODE == 1) {
+          const float pm = pc_mult<float>(pcc, wavenum(kx, NN), col.wy, col.wz);
+          val.x *= pm;
+          val.y *= pm;
+          if (!first) {
+            const float2 po = P[idx];
+            val.x += bc * po.x;
+            val.y += bc * po.y;
+          }
+          P[idx] = val;
+        }
+        v[m][a] = val;
+      }
+    }
+#pragma unroll 1
+    for (int j = 0; j < 3; j++) {
+#pragma unroll
+      for (int m = 0; m < NB1; m++) {
+        const int b = gi + GR * m;
+        float2 u[R1];
+#pragma unroll
+        for (int a = 0; a < R1; a++) {
+          const int kx = R2 * a + b;
+          const float w = (float)(j == 0 ? wavenum(kx, NN) : (j == 1 ? col.wy : col.wz)) * invN;
+          u[a] = make_float2(-w * v[m][a].y, w * v[m][a].x);
+        }
+        reg_dft<R1, +1>(u);
+#pragma unroll
+        for (int k1 = 0; k1 < R1; k1++) {
+          if (k1) u[k1] = cmul2(u[k1], tw_n<NN, +1>(tw, b * k1));
+          sm[(k1 * R2 + b) * T + c] = u[k1];
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int m2 = 0; m2 < NB2; m2++) {
+        const int k1 = gi + GR * m2;
+        float2 y[R2];
+#pragma unroll
+        for (int b = 0; b < R2; b++) y[b] = sm[(k1 * R2 + b) * T + c];
+        reg_dft<R2, +1>(y);
+#pragma unroll
+        for (int k2 = 0; k2 < R2; k2++)
+          Gc[(int64_t)j * g.Ns + (int64_t)(k1 + R1 * k2) * plane + col.q] = y[k2];
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Forward transforms along x of the three spectra of k grad u, divergence, and the epilogue of
+// k_spec_div (same arguments and scalar semantics).
+template <int NN, int EPI>
+__global__ void __launch_bounds__(256, 2)
+    k_xfwd(Geo g, const float* __restrict__ G3, const float* __restrict__ aux_in,
+           const float* __restrict__ cx, float* __restrict__ out, float* __restrict__ aux_out,
+           float scale, DevScalars* __restrict__ sc, RedWs ws, const float2* __restrict__ tw_g) {
+  using D = XDecomp<NN>;
+  constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
+  constexpr int NB1 = R2 / GR, NB2 = R1 / GR;
+  __shared__ float2 sm[NN * T];
+  __shared__ float2 tw[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw_g[i];
+  __syncthreads();
+  if (EPI == EPI_CGW && sc->status != 0) return;
+  const int c = threadIdx.x % T, gi = threadIdx.x / T;
+  const int64_t plane = (int64_t)g.n * g.nh;
+  const int ntiles = (int)(plane / T);
+  const float a = EPI == EPI_APPLYD ? 0.f : (float)sc->a_cn;
+  const float pcc = (float)sc->pc_c;
+  const float invN = (float)g.invN;
+  const float2* Gc = reinterpret_cast<const float2*>(G3);
+  const float2* AX = reinterpret_cast<const float2*>(aux_in);
+  const float2* CX = reinterpret_cast<const float2*>(cx);
+  float2* O = reinterpret_cast<float2*>(out);
+  float2* AO = reinterpret_cast<float2*>(aux_out);
+  Acc<float> acc[4];
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const XCol col = xcol(g, (int64_t)tile * T + c);
+    float2 dsum[NB2][R2];
+#pragma unroll
+    for (int m2 = 0; m2 < NB2; m2++)
+#pragma unroll
+      for (int k2 = 0; k2 < R2; k2++) dsum[m2][k2] = make_float2(0.f, 0.f);
+#pragma unroll 1
+    for (int j = 0; j < 3; j++) {
+#pragma unroll
+      for (int m = 0; m < NB1; m++) {
+        const int b = gi + GR * m;
+        float2 u[R1];
+#pragma unroll
+        for (int a1 = 0; a1 < R1; a1++)
+          u[a1] = Gc[(int64_t)j * g.Ns + (int64_t)(R2 * a1 + b) * plane + col.q];
+        reg_dft<R1, -1>(u);
+#pragma unroll
+        for (int k1 = 0; k1 < R1; k1++) {
+          if (k1) u[k1] = cmul2(u[k1], tw_n<NN, -1>(tw, b * k1));
+          sm[(k1 * R2 + b) * T + c] = u[k1];
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int m2 = 0; m2 < NB2; m2++) {
+        const int k1 = gi + GR * m2;
+        float2 y[R2];
+#pragma unroll
+        for (int b = 0; b < R2; b++) y[b] = sm[(k1 * R2 + b) * T + c];
+        reg_dft<R2, -1>(y);
+#pragma unroll
+        for (int k2 = 0; k2 < R2; k2++) {
+          const int kx = k1 + R1 * k2;
+          const float w = (float)(j == 0 ? wavenum(kx, NN) : (j == 1 ? col.wy : col.wz));
+          dsum[m2][k2].x -= w * y[k2].y;  // i w F
+          dsum[m2][k2].y += w * y[k2].x;
+        }
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int m2 = 0; m2 < NB2; m2++) {
+      const int k1 = gi + GR * m2;
+#pragma unroll
+      for (int k2 = 0; k2 < R2; k2++) {
+        const int kx = k1 + R1 * k2;
+        const int64_t idx = (int64_t)kx * plane + col.q;
+        const float2 d = dsum[m2][k2];
+        if (EPI == EPI_APPLYD) {
+          O[idx] = make_float2(d.x * scale, d.y * scale);
+        } else if (EPI == EPI_SETUP) {
+          const float2 cv = AX[idx];
+          const float br = cv.x + a * d.x, bi = cv.y + a * d.y;
+          const float rr = 2.f * a * d.x, ri = 2.f * a * d.y;
+          const float pm = pc_mult<float>(pcc, wavenum(kx, NN), col.wy, col.wz);
+          const float r2 = rr * rr + ri * ri;
+          acc[0].add(col.mult * pm * pm * (br * br + bi * bi));
+          acc[1].add(col.mult * pm * pm * r2);
+          acc[2].add(col.mult * pm * r2);
+          if (CX) {
+            const float2 xv = CX[idx];
+            acc[3].add(col.mult * (xv.x * d.x + xv.y * d.y));
+          }
+          O[idx] = make_float2(cv.x * invN, cv.y * invN);
+          AO[idx] = make_float2(rr, ri);
+        } else {  // EPI_CGW
+          const float2 p = AX[idx];
+          const float wr = p.x - a * d.x, wi = p.y - a * d.y;
+          acc[0].add(col.mult * (p.x * wr + p.y * wi));
+          O[idx] = make_float2(wr, wi);
+        }
+      }
+    }
+  }
+  if constexpr (EPI == EPI_SETUP) {
+    double sums[4] = {acc[0].value(), acc[1].value(), acc[2].value(), acc[3].value()};
+    if (!grid_sum_last<4>(sums, ws)) return;
+    if (threadIdx.x == 0) div_setup_finish(sums, sc, g.invN, cx != nullptr);
+  } else if constexpr (EPI == EPI_CGW) {
+    double sums[1] = {acc[0].value()};
+    if (!grid_sum_last<1>(sums, ws)) return;
+    if (threadIdx.x == 0) div_cgw_finish(sums[0], sc, g.invN);
+  }
+}
+
+}  // namespace glia

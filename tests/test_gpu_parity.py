@@ -234,3 +234,26 @@ def test_repeated_adjoint_after_one_state_solve_checkpointed():
     configure(f, wl, tissue, centers)
     f.solve_state(f.phi_apply(np.linspace(0.2, 1.0, len(centers))))
     assert rel_l2(a, f.solve_adjoint(pt)) < 1e-12
+
+
+@pytest.mark.parametrize("n", [64, 128, 256])
+def test_xpass_matches_cufft_3d_path(n, monkeypatch):
+    """FP32 D apply, state solve and gradient with the x transform fused into the spectral
+    kernels (k_xinv / k_xfwd around batched 2-D cuFFT) against the 3-D cuFFT path."""
+    nt = 3
+    wl, tissue, centers = small_problem(n, nt, n_gauss=8)
+    d1 = observation(wl, tissue, centers)
+    f = reference_test_field(n) + 0.1 * tissue.wm.reshape(-1)
+    x = np.concatenate([np.linspace(0.1, 0.9, len(centers)), [wl.kappa, wl.rho]])
+    out = []
+    for on in ("1", "0"):
+        monkeypatch.setenv("GLIA_XPASS", on)
+        g = gpu(n, MIXED)
+        configure(g, wl, tissue, centers)
+        g.set_obs_filter(np.ones(n ** 3))
+        c0 = g.phi_apply(np.linspace(0.2, 1.0, len(centers)))
+        out.append((g.apply_d(f), g.solve_state(c0), g.eval_objective_and_gradient(x, d1)))
+    assert rel_l2(out[0][0], out[1][0]) < 2e-6
+    assert rel_l2(out[0][1], out[1][1]) < 1e-5
+    assert abs(out[0][2][0] - out[1][2][0]) <= 1e-5 * abs(out[1][2][0])
+    assert rel_l2(out[0][2][1], out[1][2][1]) < 1e-4
