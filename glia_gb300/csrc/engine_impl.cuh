@@ -398,18 +398,35 @@ class Engine final : public EngineBase {
     if constexpr (std::is_same<R, float>::value) {
       constexpr int MODE = CGDIR ? 1 : 0;
       const int n = g_.n;
+      const int grid = std::min(xres_inv_, pw_blocks_);
       if (n == 256)
-        k_xinv<256, MODE><<<pw_blocks_, 256, 0, stream_>>>(g_, src, pdir, g3s_, sc_, tw256_);
+        k_xinv<256, MODE><<<grid, 256, 0, stream_>>>(g_, src, pdir, g3s_, sc_, tw256_);
       else if (n == 128)
-        k_xinv<128, MODE><<<pw_blocks_, 256, 0, stream_>>>(g_, src, pdir, g3s_, sc_, tw256_);
+        k_xinv<128, MODE><<<grid, 256, 0, stream_>>>(g_, src, pdir, g3s_, sc_, tw256_);
       else
-        k_xinv<64, MODE><<<pw_blocks_, 256, 0, stream_>>>(g_, src, pdir, g3s_, sc_, tw256_);
+        k_xinv<64, MODE><<<grid, 256, 0, stream_>>>(g_, src, pdir, g3s_, sc_, tw256_);
+    }
+  }
+  // resident CTAs of the x-pass kernels on this device (persistent grids: every CTA walks the
+  // same number of tiles to within one)
+  template <int NN>
+  void init_xpass_grids() {
+    if constexpr (std::is_same<R, float>::value) {
+      auto per_sm = [](auto kern) {
+        int b = 0;
+        GLIA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 256, 0));
+        return std::max(1, std::min(b, kMaxRedBlocksPerSm));
+      };
+      xres_inv_ = sms_ * std::min(per_sm(k_xinv<NN, 0>), per_sm(k_xinv<NN, 1>));
+      xres_fwd_ = sms_ * std::min({per_sm(k_xfwd<NN, EPI_APPLYD>), per_sm(k_xfwd<NN, EPI_SETUP>),
+                                   per_sm(k_xfwd<NN, EPI_CGW>)});
     }
   }
   template <int EPI>
   void launch_xfwd(const R* aux_in, const R* cx, R* out, R* aux_out, R scale, int blocks) {
     if constexpr (std::is_same<R, float>::value) {
       const int n = g_.n;
+      blocks = std::min(xres_fwd_, blocks);
       if (n == 256)
         k_xfwd<256, EPI><<<blocks, 256, 0, stream_>>>(g_, g3s_, aux_in, cx, out, aux_out, scale,
                                                       sc_, ws_, tw256_);
@@ -1436,6 +1453,12 @@ class Engine final : public EngineBase {
       }
       tw256_ = dalloc<float2>(256);
       GLIA_CUDA(cudaMemcpy(tw256_, tw.data(), 256 * sizeof(float2), cudaMemcpyHostToDevice));
+      if (n == 256)
+        init_xpass_grids<256>();
+      else if (n == 128)
+        init_xpass_grids<128>();
+      else
+        init_xpass_grids<64>();
     }
     fft_ws_bytes_ = std::max({w[0], w[1], w[2], w[3], w[4], w2[0], w2[1], (size_t)16});
     fft_ws_ = dalloc<char>((int64_t)fft_ws_bytes_);
@@ -1625,6 +1648,7 @@ class Engine final : public EngineBase {
   bool xpass_ = false;   // x pass fused into the spectral kernels (FP32, n = 64 ... 256)
   cufftHandle r2c2d3_ = 0, c2r2d3_ = 0;  // batched 2-D (y, z) transforms, 3n planes
   float2* tw256_ = nullptr;
+  int xres_inv_ = 0, xres_fwd_ = 0;  // resident CTAs of k_xinv / k_xfwd on this device
   float2* tw_ = nullptr;
   char* fft_ws_ = nullptr;
   char* batch_ws_ = nullptr;

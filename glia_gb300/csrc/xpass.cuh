@@ -5,13 +5,16 @@
 // along x. cuFFT does the (y, z) part as a contiguous batched 2-D transform; these kernels do the
 // x part inside the passes around it:
 //  k_xinv: new PCG direction p = P r + b p (or a plain spectrum), the three gradient spectra
-//          i w_j p / N, and their inverse transforms along x -> G_j(x, ky, kz);
+//          i w_j p / N and their inverse transforms along x -> G_j(x, ky, kz) (two transforms);
 //  k_xfwd: forward transforms along x of the three spectra of k grad p, the divergence
-//          sum_j i w_j F_j, and the epilogue of k_spec_div (CG operator / solve set-up / plain D).
+//          sum_j i w_j F_j (two transforms), and the epilogue of k_spec_div (CG operator / solve
+//          set-up / plain D).
 // Each CTA owns a tile: all n rows along x times T consecutive (ky, kz) columns of the flattened
 // (ky, kz) plane (T complex = 128 to 512 contiguous bytes per row). The n-point DFT along x is
 // R1 x R2: an R1-point DFT in registers over x = R2 a + b, a twiddle exp(s 2 pi i b k1 / n), one
 // exchange through shared memory, and an R2-point DFT in registers giving k = k1 + R1 k2.
+// Indices are 32-bit: 3 n^2 (n/2 + 1) < 2^31 for n <= 256. The grid is persistent (the resident
+// CTA count), so every CTA walks the same number of tiles to within one.
 #pragma once
 
 #include "kernels.cuh"
@@ -96,11 +99,11 @@ __device__ __forceinline__ float2 tw_n(const float2* tw, int e) {
 
 // Column geometry of a tile: flattened (ky, kz) index q, its wave numbers and multiplicity.
 struct XCol {
-  int64_t q;
+  int q;
   int wy, wz;
   float mult;
 };
-__device__ __forceinline__ XCol xcol(const Geo& g, int64_t q) {
+__device__ __forceinline__ XCol xcol(const Geo& g, int q) {
   XCol c;
   c.q = q;
   const uint32_t ky = g.fd_nh.div((uint32_t)q);
@@ -111,22 +114,61 @@ __device__ __forceinline__ XCol xcol(const Geo& g, int64_t q) {
   return c;
 }
 
+// One n-point DFT along x of this thread's column, sign S: in(m, b, a) is the input at
+// x = R2 a + b, out(m2, k1, k2, y) receives X[k1 + R1 k2]. All threads of the CTA take part
+// (two barriers).
+template <int NN, int S, class In, class Out>
+__device__ __forceinline__ void xdft(float2* sm, const float2* tw, int c, int gi, In&& in,
+                                     Out&& out) {
+  using D = XDecomp<NN>;
+  constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
+  constexpr int NB1 = R2 / GR, NB2 = R1 / GR;
+#pragma unroll
+  for (int m = 0; m < NB1; m++) {
+    const int b = gi + GR * m;
+    float2 u[R1];
+#pragma unroll
+    for (int a = 0; a < R1; a++) u[a] = in(m, b, a);
+    reg_dft<R1, S>(u);
+#pragma unroll
+    for (int k1 = 0; k1 < R1; k1++) {
+      if (k1) u[k1] = cmul2(u[k1], tw_n<NN, S>(tw, b * k1));
+      sm[(k1 * R2 + b) * T + c] = u[k1];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int m2 = 0; m2 < NB2; m2++) {
+    const int k1 = gi + GR * m2;
+    float2 y[R2];
+#pragma unroll
+    for (int b = 0; b < R2; b++) y[b] = sm[(k1 * R2 + b) * T + c];
+    reg_dft<R2, S>(y);
+#pragma unroll
+    for (int k2 = 0; k2 < R2; k2++) out(m2, k1, k2, y[k2]);
+  }
+  __syncthreads();
+}
+
 // MODE 0: spectrum src -> G; MODE 1: PCG direction p = P r + b p (r = src, p = pdir, p written).
+// The y and z gradient spectra differ from the plain spectrum only by factors constant along x,
+// so two x transforms give the three components: G_x = F^-1(i w_x u) / N and
+// G_y, G_z = i w_y, i w_z F^-1(u) / N.
 template <int NN, int MODE>
 __global__ void __launch_bounds__(256, 2)
     k_xinv(Geo g, const float* __restrict__ src, float* __restrict__ pdir, float* __restrict__ G3,
            const DevScalars* __restrict__ sc, const float2* __restrict__ tw_g) {
   using D = XDecomp<NN>;
   constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
-  constexpr int NB1 = R2 / GR, NB2 = R1 / GR;
+  constexpr int NB1 = R2 / GR;
   __shared__ float2 sm[NN * T];
   __shared__ float2 tw[256];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw_g[i];
   __syncthreads();
   if (MODE == 1 && sc->status != 0) return;
   const int c = threadIdx.x % T, gi = threadIdx.x / T;
-  const int64_t plane = (int64_t)g.n * g.nh;
-  const int ntiles = (int)(plane / T);
+  const int plane = NN * g.nh, Ns = plane * NN;
+  const int ntiles = plane / T;
   const float invN = (float)g.invN;
   const bool first = MODE == 1 ? sc->iter == 0 : true;
   const float bc = MODE == 1 ? (float)sc->bcoef : 0.f;
@@ -135,7 +177,7 @@ __global__ void __launch_bounds__(256, 2)
   float2* P = reinterpret_cast<float2*>(pdir);
   float2* Gc = reinterpret_cast<float2*>(G3);
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const XCol col = xcol(g, (int64_t)tile * T + c);
+    const XCol col = xcol(g, tile * T + c);
     float2 v[NB1][R1];
 #pragma unroll
     for (int m = 0; m < NB1; m++) {
@@ -143,7 +185,7 @@ __global__ void __launch_bounds__(256, 2)
 #pragma unroll
       for (int a = 0; a < R1; a++) {
         const int kx = R2 * a + b;
-        const int64_t idx = (int64_t)kx * plane + col.q;
+        const int idx = kx * plane + col.q;
         float2 val = S[idx];
         if (MODE == 1) {
           const float pm = pc_mult<float>(pcc, wavenum(kx, NN), col.wy, col.wz);
@@ -159,44 +201,27 @@ __global__ void __launch_bounds__(256, 2)
         v[m][a] = val;
       }
     }
-#pragma unroll 1
-    for (int j = 0; j < 3; j++) {
-#pragma unroll
-      for (int m = 0; m < NB1; m++) {
-        const int b = gi + GR * m;
-        float2 u[R1];
-#pragma unroll
-        for (int a = 0; a < R1; a++) {
-          const int kx = R2 * a + b;
-          const float w = (float)(j == 0 ? wavenum(kx, NN) : (j == 1 ? col.wy : col.wz)) * invN;
-          u[a] = make_float2(-w * v[m][a].y, w * v[m][a].x);
-        }
-        reg_dft<R1, +1>(u);
-#pragma unroll
-        for (int k1 = 0; k1 < R1; k1++) {
-          if (k1) u[k1] = cmul2(u[k1], tw_n<NN, +1>(tw, b * k1));
-          sm[(k1 * R2 + b) * T + c] = u[k1];
-        }
-      }
-      __syncthreads();
-#pragma unroll
-      for (int m2 = 0; m2 < NB2; m2++) {
-        const int k1 = gi + GR * m2;
-        float2 y[R2];
-#pragma unroll
-        for (int b = 0; b < R2; b++) y[b] = sm[(k1 * R2 + b) * T + c];
-        reg_dft<R2, +1>(y);
-#pragma unroll
-        for (int k2 = 0; k2 < R2; k2++)
-          Gc[(int64_t)j * g.Ns + (int64_t)(k1 + R1 * k2) * plane + col.q] = y[k2];
-      }
-      __syncthreads();
-    }
+    xdft<NN, +1>(
+        sm, tw, c, gi,
+        [&](int m, int b, int a) {
+          const float w = (float)wavenum(R2 * a + b, NN) * invN;
+          return make_float2(-w * v[m][a].y, w * v[m][a].x);
+        },
+        [&](int, int k1, int k2, float2 y) { Gc[(k1 + R1 * k2) * plane + col.q] = y; });
+    const float fy = (float)col.wy * invN, fz = (float)col.wz * invN;
+    xdft<NN, +1>(
+        sm, tw, c, gi, [&](int m, int, int a) { return v[m][a]; },
+        [&](int, int k1, int k2, float2 y) {
+          const int i = (k1 + R1 * k2) * plane + col.q;
+          Gc[Ns + i] = make_float2(-fy * y.y, fy * y.x);
+          Gc[2 * Ns + i] = make_float2(-fz * y.y, fz * y.x);
+        });
   }
 }
 
-// Forward transforms along x of the three spectra of k grad u, divergence, and the epilogue of
-// k_spec_div (same arguments and scalar semantics).
+// Forward transforms along x of the three spectra F_j of k grad u, the divergence
+// sum_j i w_j F_j = i w_x F(K_x) + F(i w_y K_y + i w_z K_z) (two x transforms), and the epilogue
+// of k_spec_div (same arguments and scalar semantics).
 template <int NN, int EPI>
 __global__ void __launch_bounds__(256, 2)
     k_xfwd(Geo g, const float* __restrict__ G3, const float* __restrict__ aux_in,
@@ -204,15 +229,15 @@ __global__ void __launch_bounds__(256, 2)
            float scale, DevScalars* __restrict__ sc, RedWs ws, const float2* __restrict__ tw_g) {
   using D = XDecomp<NN>;
   constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
-  constexpr int NB1 = R2 / GR, NB2 = R1 / GR;
+  constexpr int NB2 = R1 / GR;
   __shared__ float2 sm[NN * T];
   __shared__ float2 tw[256];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw_g[i];
   __syncthreads();
   if (EPI == EPI_CGW && sc->status != 0) return;
   const int c = threadIdx.x % T, gi = threadIdx.x / T;
-  const int64_t plane = (int64_t)g.n * g.nh;
-  const int ntiles = (int)(plane / T);
+  const int plane = NN * g.nh, Ns = plane * NN;
+  const int ntiles = plane / T;
   const float a = EPI == EPI_APPLYD ? 0.f : (float)sc->a_cn;
   const float pcc = (float)sc->pc_c;
   const float invN = (float)g.invN;
@@ -223,53 +248,33 @@ __global__ void __launch_bounds__(256, 2)
   float2* AO = reinterpret_cast<float2*>(aux_out);
   Acc<float> acc[4];
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const XCol col = xcol(g, (int64_t)tile * T + c);
+    const XCol col = xcol(g, tile * T + c);
     float2 dsum[NB2][R2];
-#pragma unroll
-    for (int m2 = 0; m2 < NB2; m2++)
-#pragma unroll
-      for (int k2 = 0; k2 < R2; k2++) dsum[m2][k2] = make_float2(0.f, 0.f);
-#pragma unroll 1
-    for (int j = 0; j < 3; j++) {
-#pragma unroll
-      for (int m = 0; m < NB1; m++) {
-        const int b = gi + GR * m;
-        float2 u[R1];
-#pragma unroll
-        for (int a1 = 0; a1 < R1; a1++)
-          u[a1] = Gc[(int64_t)j * g.Ns + (int64_t)(R2 * a1 + b) * plane + col.q];
-        reg_dft<R1, -1>(u);
-#pragma unroll
-        for (int k1 = 0; k1 < R1; k1++) {
-          if (k1) u[k1] = cmul2(u[k1], tw_n<NN, -1>(tw, b * k1));
-          sm[(k1 * R2 + b) * T + c] = u[k1];
-        }
-      }
-      __syncthreads();
-#pragma unroll
-      for (int m2 = 0; m2 < NB2; m2++) {
-        const int k1 = gi + GR * m2;
-        float2 y[R2];
-#pragma unroll
-        for (int b = 0; b < R2; b++) y[b] = sm[(k1 * R2 + b) * T + c];
-        reg_dft<R2, -1>(y);
-#pragma unroll
-        for (int k2 = 0; k2 < R2; k2++) {
-          const int kx = k1 + R1 * k2;
-          const float w = (float)(j == 0 ? wavenum(kx, NN) : (j == 1 ? col.wy : col.wz));
-          dsum[m2][k2].x -= w * y[k2].y;  // i w F
-          dsum[m2][k2].y += w * y[k2].x;
-        }
-      }
-      __syncthreads();
-    }
+    xdft<NN, -1>(
+        sm, tw, c, gi, [&](int, int b, int a1) { return Gc[(R2 * a1 + b) * plane + col.q]; },
+        [&](int m2, int k1, int k2, float2 y) {
+          const float w = (float)wavenum(k1 + R1 * k2, NN);
+          dsum[m2][k2] = make_float2(-w * y.y, w * y.x);
+        });
+    const float wy = (float)col.wy, wz = (float)col.wz;
+    xdft<NN, -1>(
+        sm, tw, c, gi,
+        [&](int, int b, int a1) {
+          const int i = (R2 * a1 + b) * plane + col.q;
+          const float2 gy = Gc[Ns + i], gz = Gc[2 * Ns + i];
+          return make_float2(-(wy * gy.y + wz * gz.y), wy * gy.x + wz * gz.x);
+        },
+        [&](int m2, int, int k2, float2 y) {
+          dsum[m2][k2].x += y.x;
+          dsum[m2][k2].y += y.y;
+        });
 #pragma unroll
     for (int m2 = 0; m2 < NB2; m2++) {
       const int k1 = gi + GR * m2;
 #pragma unroll
       for (int k2 = 0; k2 < R2; k2++) {
         const int kx = k1 + R1 * k2;
-        const int64_t idx = (int64_t)kx * plane + col.q;
+        const int idx = kx * plane + col.q;
         const float2 d = dsum[m2][k2];
         if (EPI == EPI_APPLYD) {
           O[idx] = make_float2(d.x * scale, d.y * scale);
