@@ -400,11 +400,14 @@ class Engine final : public EngineBase {
       const int n = g_.n;
       const int grid = std::min(xres_inv_, pw_blocks_);
       if (n == 256)
-        k_xinv<256, MODE><<<grid, 256, 0, stream_>>>(g_, src, pdir, g3s_, sc_, tw256_);
+        k_xinv<256, MODE><<<grid, 256, xinv_smem_bytes<256, MODE>(), stream_>>>(
+            g_, src, pdir, g3s_, sc_, tw256_);
       else if (n == 128)
-        k_xinv<128, MODE><<<grid, 256, 0, stream_>>>(g_, src, pdir, g3s_, sc_, tw256_);
+        k_xinv<128, MODE><<<grid, 256, xinv_smem_bytes<128, MODE>(), stream_>>>(
+            g_, src, pdir, g3s_, sc_, tw256_);
       else
-        k_xinv<64, MODE><<<grid, 256, 0, stream_>>>(g_, src, pdir, g3s_, sc_, tw256_);
+        k_xinv<64, MODE><<<grid, 256, xinv_smem_bytes<64, MODE>(), stream_>>>(
+            g_, src, pdir, g3s_, sc_, tw256_);
     }
   }
   // resident CTAs of the x-pass kernels on this device (persistent grids: every CTA walks the
@@ -412,14 +415,17 @@ class Engine final : public EngineBase {
   template <int NN>
   void init_xpass_grids() {
     if constexpr (std::is_same<R, float>::value) {
-      auto per_sm = [](auto kern) {
+      auto per_sm = [](auto kern, int smem) {
+        if (smem > 48 * 1024)
+          GLIA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         int b = 0;
-        GLIA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 256, 0));
+        GLIA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 256, smem));
         return std::max(1, std::min(b, kMaxRedBlocksPerSm));
       };
-      xres_inv_ = sms_ * std::min(per_sm(k_xinv<NN, 0>), per_sm(k_xinv<NN, 1>));
-      xres_fwd_ = sms_ * std::min({per_sm(k_xfwd<NN, EPI_APPLYD>), per_sm(k_xfwd<NN, EPI_SETUP>),
-                                   per_sm(k_xfwd<NN, EPI_CGW>)});
+      xres_inv_ = sms_ * std::min(per_sm(k_xinv<NN, 0>, xinv_smem_bytes<NN, 0>()),
+                                  per_sm(k_xinv<NN, 1>, xinv_smem_bytes<NN, 1>()));
+      xres_fwd_ = sms_ * std::min({per_sm(k_xfwd<NN, EPI_APPLYD>, 0),
+                                   per_sm(k_xfwd<NN, EPI_SETUP>, 0), per_sm(k_xfwd<NN, EPI_CGW>, 0)});
     }
   }
   template <int EPI>

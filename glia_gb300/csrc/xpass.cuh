@@ -97,6 +97,40 @@ __device__ __forceinline__ float2 tw_n(const float2* tw, int e) {
   return w;
 }
 
+// Asynchronous 16-byte global -> shared copies (cp.async, completion by commit / wait groups).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Stages tile `tile` of src (NN rows of T complex, rows `plane` complex apart) into shared memory
+// as slot[row * T + col]: 2048 16-byte chunks, eight per thread, consecutive threads on
+// consecutive chunks of a row.
+template <int NN, int T>
+__device__ __forceinline__ void stage_tile(float2* slot, const float2* src, int plane, int tile) {
+  constexpr int CR = T / 2, NCH = NN * CR;
+  static_assert(NCH % 256 == 0, "tile chunks must divide over 256 threads");
+#pragma unroll
+  for (int j = 0; j < NCH / 256; j++) {
+    const int e = (int)threadIdx.x + 256 * j;
+    const int row = e / CR, ch = e - row * CR;
+    cp_async16(slot + row * T + 2 * ch, src + row * plane + tile * T + 2 * ch);
+  }
+}
+
+// Dynamic shared memory of k_xinv: input slots (1 or 2), the exchange buffer, the twiddles.
+template <int NN, int MODE>
+constexpr int xinv_smem_bytes() {
+  return ((MODE == 1 ? 3 : 2) * NN * XDecomp<NN>::T + 256) * (int)sizeof(float2);
+}
+
 // Column geometry of a tile: flattened (ky, kz) index q, its wave numbers and multiplicity.
 struct XCol {
   int q;
@@ -153,7 +187,8 @@ __device__ __forceinline__ void xdft(float2* sm, const float2* tw, int c, int gi
 // MODE 0: spectrum src -> G; MODE 1: PCG direction p = P r + b p (r = src, p = pdir, p written).
 // The y and z gradient spectra differ from the plain spectrum only by factors constant along x,
 // so two x transforms give the three components: G_x = F^-1(i w_x u) / N and
-// G_y, G_z = i w_y, i w_z F^-1(u) / N.
+// G_y, G_z = i w_y, i w_z F^-1(u) / N. The inputs of the CTA's next tile are staged into shared
+// memory (cp.async) while the current tile is transformed.
 template <int NN, int MODE>
 __global__ void __launch_bounds__(256, 2)
     k_xinv(Geo g, const float* __restrict__ src, float* __restrict__ pdir, float* __restrict__ G3,
@@ -161,11 +196,13 @@ __global__ void __launch_bounds__(256, 2)
   using D = XDecomp<NN>;
   constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
   constexpr int NB1 = R2 / GR;
-  __shared__ float2 sm[NN * T];
-  __shared__ float2 tw[256];
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw_g[i];
-  __syncthreads();
+  extern __shared__ float4 xinv_dyn[];
+  float2* slotS = reinterpret_cast<float2*>(xinv_dyn);
+  float2* slotP = slotS + NN * T;
+  float2* sm = slotP + (MODE == 1 ? NN * T : 0);
+  float2* tw = sm + NN * T;
   if (MODE == 1 && sc->status != 0) return;
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw_g[i];
   const int c = threadIdx.x % T, gi = threadIdx.x / T;
   const int plane = NN * g.nh, Ns = plane * NN;
   const int ntiles = plane / T;
@@ -176,7 +213,17 @@ __global__ void __launch_bounds__(256, 2)
   const float2* S = reinterpret_cast<const float2*>(src);
   float2* P = reinterpret_cast<float2*>(pdir);
   float2* Gc = reinterpret_cast<float2*>(G3);
+  auto stage = [&](int t) {
+    if (t < ntiles) {
+      stage_tile<NN, T>(slotS, S, plane, t);
+      if (MODE == 1 && !first) stage_tile<NN, T>(slotP, P, plane, t);
+    }
+    cp_async_commit();
+  };
+  stage(blockIdx.x);
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    cp_async_wait<0>();
+    __syncthreads();
     const XCol col = xcol(g, tile * T + c);
     float2 v[NB1][R1];
 #pragma unroll
@@ -185,22 +232,23 @@ __global__ void __launch_bounds__(256, 2)
 #pragma unroll
       for (int a = 0; a < R1; a++) {
         const int kx = R2 * a + b;
-        const int idx = kx * plane + col.q;
-        float2 val = S[idx];
+        float2 val = slotS[kx * T + c];
         if (MODE == 1) {
           const float pm = pc_mult<float>(pcc, wavenum(kx, NN), col.wy, col.wz);
           val.x *= pm;
           val.y *= pm;
           if (!first) {
-            const float2 po = P[idx];
+            const float2 po = slotP[kx * T + c];
             val.x += bc * po.x;
             val.y += bc * po.y;
           }
-          P[idx] = val;
+          P[kx * plane + col.q] = val;
         }
         v[m][a] = val;
       }
     }
+    __syncthreads();  // slots read: stage the next tile behind the transforms
+    stage(tile + gridDim.x);
     xdft<NN, +1>(
         sm, tw, c, gi,
         [&](int m, int b, int a) {
@@ -217,6 +265,7 @@ __global__ void __launch_bounds__(256, 2)
           Gc[2 * Ns + i] = make_float2(-fz * y.y, fz * y.x);
         });
   }
+  cp_async_wait<0>();
 }
 
 // Forward transforms along x of the three spectra F_j of k grad u, the divergence
