@@ -24,7 +24,7 @@
 #include "kernels.cuh"
 #include "ktimer.cuh"
 #include "zpass.cuh"
-#include "xpass.cuh"
+#include "ownfft.cuh"
 
 #define GLIA_TIMED(slot, bytes, ...)             \
   do {                                           \
@@ -164,7 +164,7 @@ class Engine final : public EngineBase {
     stream_ = s ? (cudaStream_t)s : own_stream_;
     for (cufftHandle p : {r2c1_, c2r1_, r2c3_, c2r3_}) GLIA_CUFFT(cufftSetStream(p, stream_));
     if (zpass_) GLIA_CUFFT(cufftSetStream(p2d_, stream_));
-    if (xpass_)
+    if (xpass_ && !own_)
       for (cufftHandle p : {r2c2d3_, c2r2d3_}) GLIA_CUFFT(cufftSetStream(p, stream_));
   }
   void synchronize() override { GLIA_CUDA(cudaStreamSynchronize(stream_)); }
@@ -365,6 +365,13 @@ class Engine final : public EngineBase {
   // it is the full 3-D spectrum.
   template <bool CGDIR>
   void d_front(const R* src, R* pdir) {
+    if (own_) {  // no cuFFT: x, y, z passes of our own, k multiplied inside the z pass
+      GLIA_TIMED(KS_XINV, SB() * (CGDIR ? 5 : 3), launch_xinv<CGDIR>(src, pdir));
+      GLIA_TIMED(KS_YINV, SB() * 2 + FB() * 3, launch_own(0));
+      GLIA_TIMED(KS_ZFUSED, FB() * 7, launch_own(1));
+      GLIA_TIMED(KS_YFWD, FB() * 3 + SB() * 2, launch_own(2));
+      return;
+    }
     if (xpass_) {
       GLIA_TIMED(KS_XINV, SB() * (CGDIR ? 6 : 4), launch_xinv<CGDIR>(src, pdir));
       c2r(c2r2d3_, g3s_, g3r_, 3);
@@ -380,38 +387,88 @@ class Engine final : public EngineBase {
   // (k_spec_div semantics: EPI_APPLYD out = scale D; EPI_SETUP solve set-up; EPI_CGW w = A p).
   template <int EPI>
   void d_back(const R* aux_in, const R* cx, R* out, R* aux_out, R scale) {
-    const double bytes = EPI == EPI_APPLYD ? SB() * 4
-                         : EPI == EPI_SETUP ? SB() * (cx ? 7 : 6)
-                                            : SB() * 5;
+    const double nin = own_ ? 2 : 3;  // gradient blocks read by the divergence
+    const double bytes = EPI == EPI_APPLYD ? SB() * (nin + 1)
+                         : EPI == EPI_SETUP ? SB() * (nin + (cx ? 4 : 3))
+                                            : SB() * (nin + 2);
     const int slot = EPI == EPI_APPLYD ? KS_DIV_APPLYD : (EPI == EPI_SETUP ? KS_DIV_SETUP : KS_DIV_CGW);
     const int blocks = EPI == EPI_APPLYD ? pw_blocks_ : red_blocks_;
     if (xpass_) {
-      GLIA_TIMED(slot, bytes, launch_xfwd<EPI>(aux_in, cx, out, aux_out, scale, blocks));
+      const int xslot = EPI == EPI_APPLYD ? KS_XFWD_APPLYD
+                        : (EPI == EPI_SETUP ? KS_XFWD_SETUP : KS_XFWD_CGW);
+      GLIA_TIMED(xslot, bytes, launch_xfwd<EPI>(aux_in, cx, out, aux_out, scale, blocks));
       return;
     }
     GLIA_TIMED(slot, bytes,
                k_spec_div<R, EPI><<<blocks, kThreads, 0, stream_>>>(g_, g3s_, aux_in, cx, out,
                                                                     aux_out, scale, sc_, ws_));
   }
-  template <bool CGDIR>
-  void launch_xinv(const R* src, R* pdir) {
+  // x-pass and own-transform launches; kernels are instantiated per grid size (n = 64, 128, 256)
+  template <int NN, bool CGDIR, bool OUT2>
+  void xinv_n(const R* src, R* pdir, R* G) {
     if constexpr (std::is_same<R, float>::value) {
       constexpr int MODE = CGDIR ? 1 : 0;
-      const int n = g_.n;
       const int grid = std::min(xres_inv_, pw_blocks_);
-      if (n == 256)
-        k_xinv<256, MODE><<<grid, 256, xinv_smem_bytes<256, MODE>(), stream_>>>(
-            g_, src, pdir, g3s_, sc_, tw256_);
-      else if (n == 128)
-        k_xinv<128, MODE><<<grid, 256, xinv_smem_bytes<128, MODE>(), stream_>>>(
-            g_, src, pdir, g3s_, sc_, tw256_);
-      else
-        k_xinv<64, MODE><<<grid, 256, xinv_smem_bytes<64, MODE>(), stream_>>>(
-            g_, src, pdir, g3s_, sc_, tw256_);
+      k_xinv<NN, MODE, OUT2><<<grid, 256, xinv_smem_bytes<NN, MODE>(), stream_>>>(
+          g_, src, pdir, G, sc_, tw256_);
     }
   }
-  // resident CTAs of the x-pass kernels on this device (persistent grids: every CTA walks the
-  // same number of tiles to within one)
+  template <bool CGDIR>
+  void launch_xinv(const R* src, R* pdir) {
+    const int n = g_.n;
+    if (own_) {
+      if (n == 256) xinv_n<256, CGDIR, true>(src, pdir, g3r_);
+      else if (n == 128) xinv_n<128, CGDIR, true>(src, pdir, g3r_);
+      else xinv_n<64, CGDIR, true>(src, pdir, g3r_);
+    } else {
+      if (n == 256) xinv_n<256, CGDIR, false>(src, pdir, g3s_);
+      else if (n == 128) xinv_n<128, CGDIR, false>(src, pdir, g3s_);
+      else xinv_n<64, CGDIR, false>(src, pdir, g3s_);
+    }
+  }
+  template <int NN, int EPI, bool IN2>
+  void xfwd_n(const R* G, const R* aux_in, const R* cx, R* out, R* aux_out, R scale, int blocks) {
+    if constexpr (std::is_same<R, float>::value)
+      k_xfwd<NN, EPI, IN2><<<blocks, 256, 0, stream_>>>(g_, G, aux_in, cx, out, aux_out, scale,
+                                                         sc_, ws_, tw256_);
+  }
+  template <int EPI>
+  void launch_xfwd(const R* aux_in, const R* cx, R* out, R* aux_out, R scale, int blocks) {
+    const int n = g_.n;
+    blocks = std::min(xres_fwd_, blocks);
+    if (own_) {
+      if (n == 256) xfwd_n<256, EPI, true>(g3r_, aux_in, cx, out, aux_out, scale, blocks);
+      else if (n == 128) xfwd_n<128, EPI, true>(g3r_, aux_in, cx, out, aux_out, scale, blocks);
+      else xfwd_n<64, EPI, true>(g3r_, aux_in, cx, out, aux_out, scale, blocks);
+    } else {
+      if (n == 256) xfwd_n<256, EPI, false>(g3s_, aux_in, cx, out, aux_out, scale, blocks);
+      else if (n == 128) xfwd_n<128, EPI, false>(g3s_, aux_in, cx, out, aux_out, scale, blocks);
+      else xfwd_n<64, EPI, false>(g3s_, aux_in, cx, out, aux_out, scale, blocks);
+    }
+  }
+  // own y / z passes: 0 = k_yinv (g3r_ -> g3s_), 1 = k_zpass (g3s_ in place, k), 2 = k_yfwd
+  // (g3s_ -> g3r_)
+  template <int NN>
+  void own_n(int which) {
+    if constexpr (std::is_same<R, float>::value) {
+      if (which == 0)
+        k_yinv<NN><<<std::min(own_res_[0], pw_blocks_), 256, yinv_smem_bytes<NN>(), stream_>>>(
+            g3r_, g3s_, tw256_);
+      else if (which == 1)
+        k_zpass<NN><<<std::min(own_res_[1], pw_blocks_), 256, zpass_smem_bytes<NN>(), stream_>>>(
+            g3s_, kxx_, tw256_);
+      else
+        k_yfwd<NN><<<std::min(own_res_[2], pw_blocks_), 256, 0, stream_>>>(g3s_, g3r_, tw256_);
+    }
+  }
+  void launch_own(int which) {
+    const int n = g_.n;
+    if (n == 256) own_n<256>(which);
+    else if (n == 128) own_n<128>(which);
+    else own_n<64>(which);
+  }
+  // resident CTAs of the x-pass and own-transform kernels on this device (persistent grids:
+  // every CTA walks the same number of tiles to within one)
   template <int NN>
   void init_xpass_grids() {
     if constexpr (std::is_same<R, float>::value) {
@@ -422,26 +479,22 @@ class Engine final : public EngineBase {
         GLIA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 256, smem));
         return std::max(1, std::min(b, kMaxRedBlocksPerSm));
       };
-      xres_inv_ = sms_ * std::min(per_sm(k_xinv<NN, 0>, xinv_smem_bytes<NN, 0>()),
-                                  per_sm(k_xinv<NN, 1>, xinv_smem_bytes<NN, 1>()));
-      xres_fwd_ = sms_ * std::min({per_sm(k_xfwd<NN, EPI_APPLYD>, 0),
-                                   per_sm(k_xfwd<NN, EPI_SETUP>, 0), per_sm(k_xfwd<NN, EPI_CGW>, 0)});
-    }
-  }
-  template <int EPI>
-  void launch_xfwd(const R* aux_in, const R* cx, R* out, R* aux_out, R scale, int blocks) {
-    if constexpr (std::is_same<R, float>::value) {
-      const int n = g_.n;
-      blocks = std::min(xres_fwd_, blocks);
-      if (n == 256)
-        k_xfwd<256, EPI><<<blocks, 256, 0, stream_>>>(g_, g3s_, aux_in, cx, out, aux_out, scale,
-                                                      sc_, ws_, tw256_);
-      else if (n == 128)
-        k_xfwd<128, EPI><<<blocks, 256, 0, stream_>>>(g_, g3s_, aux_in, cx, out, aux_out, scale,
-                                                      sc_, ws_, tw256_);
-      else
-        k_xfwd<64, EPI><<<blocks, 256, 0, stream_>>>(g_, g3s_, aux_in, cx, out, aux_out, scale,
-                                                     sc_, ws_, tw256_);
+      if (own_) {
+        xres_inv_ = sms_ * std::min(per_sm(k_xinv<NN, 0, true>, xinv_smem_bytes<NN, 0>()),
+                                    per_sm(k_xinv<NN, 1, true>, xinv_smem_bytes<NN, 1>()));
+        xres_fwd_ = sms_ * std::min({per_sm(k_xfwd<NN, EPI_APPLYD, true>, 0),
+                                     per_sm(k_xfwd<NN, EPI_SETUP, true>, 0),
+                                     per_sm(k_xfwd<NN, EPI_CGW, true>, 0)});
+        own_res_[0] = sms_ * per_sm(k_yinv<NN>, yinv_smem_bytes<NN>());
+        own_res_[1] = sms_ * per_sm(k_zpass<NN>, zpass_smem_bytes<NN>());
+        own_res_[2] = sms_ * per_sm(k_yfwd<NN>, 0);
+      } else {
+        xres_inv_ = sms_ * std::min(per_sm(k_xinv<NN, 0, false>, xinv_smem_bytes<NN, 0>()),
+                                    per_sm(k_xinv<NN, 1, false>, xinv_smem_bytes<NN, 1>()));
+        xres_fwd_ = sms_ * std::min({per_sm(k_xfwd<NN, EPI_APPLYD, false>, 0),
+                                     per_sm(k_xfwd<NN, EPI_SETUP, false>, 0),
+                                     per_sm(k_xfwd<NN, EPI_CGW, false>, 0)});
+      }
     }
   }
 
@@ -491,7 +544,7 @@ class Engine final : public EngineBase {
       GLIA_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
       for (cufftHandle p : {r2c3_, c2r3_}) GLIA_CUFFT(cufftSetStream(p, cs));
       if (zpass_) GLIA_CUFFT(cufftSetStream(p2d_, cs));
-      if (xpass_)
+      if (xpass_ && !own_)
         for (cufftHandle p : {r2c2d3_, c2r2d3_}) GLIA_CUFFT(cufftSetStream(p, cs));
       stream_ = cs;
       GLIA_CUDA(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
@@ -517,7 +570,7 @@ class Engine final : public EngineBase {
     stream_ = saved;
     for (cufftHandle p : {r2c3_, c2r3_}) cufftSetStream(p, stream_);
     if (zpass_) cufftSetStream(p2d_, stream_);
-    if (xpass_)
+    if (xpass_ && !own_)
       for (cufftHandle p : {r2c2d3_, c2r2d3_}) cufftSetStream(p, stream_);
     if (cs) cudaStreamDestroy(cs);
     if (g) cudaGraphDestroy(g);
@@ -1434,13 +1487,16 @@ class Engine final : public EngineBase {
                                 stream_));
       GLIA_CUDA(cudaStreamSynchronize(stream_));
     }
-    // x pass fused into the spectral kernels: cuFFT does contiguous batched 2-D (y, z)
-    // transforms of the three gradient components (3n planes); default on (GLIA_XPASS=0 off)
-    const char* xoff = std::getenv("GLIA_XPASS");
+    // Transform path of the FP32 D apply at n = 64, 128, 256 (GLIA_XPASS): by default the x, y
+    // and z passes are the library's own kernels (ownfft.cuh, no cuFFT inside the PCG loop);
+    // "2d" keeps the x pass and lets cuFFT do batched 2-D (y, z) transforms with k multiplied in
+    // between; "0" uses batched 3-D cuFFT transforms.
+    const char* xenv = std::getenv("GLIA_XPASS");
     xpass_ = std::is_same<R, float>::value && (n == 64 || n == 128 || n == 256) && !zpass_ &&
-             !ref_ && !(xoff && xoff[0] == '0');
+             !ref_ && !(xenv && xenv[0] == '0');
+    own_ = xpass_ && !(xenv && std::strcmp(xenv, "2d") == 0);
     size_t w2[2] = {0, 0};
-    if (xpass_) {
+    if (xpass_ && !own_) {
       int dims[2] = {n, n};
       for (int d = 0; d < 2; d++) {
         cufftHandle& p = d == 0 ? r2c2d3_ : c2r2d3_;
@@ -1452,6 +1508,8 @@ class Engine final : public EngineBase {
                                      3 * n, &w2[d]));
         GLIA_CUFFT(cufftSetStream(p, stream_));
       }
+    }
+    if (xpass_) {
       std::vector<float2> tw(256);
       for (int j = 0; j < 256; j++) {
         const double a = -2.0 * M_PI * (double)j / 256.0;
@@ -1470,7 +1528,7 @@ class Engine final : public EngineBase {
     fft_ws_ = dalloc<char>((int64_t)fft_ws_bytes_);
     for (cufftHandle p : {r2c1_, c2r1_, r2c3_, c2r3_}) GLIA_CUFFT(cufftSetWorkArea(p, fft_ws_));
     if (zpass_) GLIA_CUFFT(cufftSetWorkArea(p2d_, fft_ws_));
-    if (xpass_)
+    if (xpass_ && !own_)
       for (cufftHandle p : {r2c2d3_, c2r2d3_}) GLIA_CUFFT(cufftSetWorkArea(p, fft_ws_));
   }
   void c2c2d(R* data, int dir) {
@@ -1655,6 +1713,8 @@ class Engine final : public EngineBase {
   cufftHandle r2c2d3_ = 0, c2r2d3_ = 0;  // batched 2-D (y, z) transforms, 3n planes
   float2* tw256_ = nullptr;
   int xres_inv_ = 0, xres_fwd_ = 0;  // resident CTAs of k_xinv / k_xfwd on this device
+  int own_res_[3] = {0, 0, 0};       // ... of k_yinv, k_zpass, k_yfwd
+  bool own_ = false;  // own y and z passes (x pass on): no cuFFT inside the D apply
   float2* tw_ = nullptr;
   char* fft_ws_ = nullptr;
   char* batch_ws_ = nullptr;

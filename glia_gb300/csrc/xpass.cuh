@@ -25,15 +25,15 @@ template <int NN>
 struct XDecomp;
 template <>
 struct XDecomp<256> {
-  static constexpr int R1 = 16, R2 = 16, T = 16;
+  static constexpr int N = 256, R1 = 16, R2 = 16, T = 16;
 };
 template <>
 struct XDecomp<128> {
-  static constexpr int R1 = 16, R2 = 8, T = 32;
+  static constexpr int N = 128, R1 = 16, R2 = 8, T = 32;
 };
 template <>
 struct XDecomp<64> {
-  static constexpr int R1 = 8, R2 = 8, T = 64;
+  static constexpr int N = 64, R1 = 8, R2 = 8, T = 64;
 };
 
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
@@ -62,11 +62,12 @@ __host__ __device__ constexpr int brev_bits(int i, int bits) {
   return r;
 }
 
-// In-register DFT of size R (8 or 16): X[k] = sum_i v[i] exp(S 2 pi i i k / R), natural order in
-// and out (iterative radix-2 on the bit-reversed copy).
+// In-register DFT of size R (2, 4, 8 or 16): X[k] = sum_i v[i] exp(S 2 pi i i k / R), natural
+// order in and out (iterative radix-2 on the bit-reversed copy).
 template <int R, int S>
 __device__ __forceinline__ void reg_dft(float2 (&v)[R]) {
-  constexpr int LOG = R == 16 ? 4 : 3;
+  static_assert(R == 2 || R == 4 || R == 8 || R == 16, "register DFT sizes 2 ... 16");
+  constexpr int LOG = R == 16 ? 4 : (R == 8 ? 3 : (R == 4 ? 2 : 1));
   float2 t[R];
 #pragma unroll
   for (int i = 0; i < R; i++) t[brev_bits(i, LOG)] = v[i];
@@ -148,14 +149,14 @@ __device__ __forceinline__ XCol xcol(const Geo& g, int q) {
   return c;
 }
 
-// One n-point DFT along x of this thread's column, sign S: in(m, b, a) is the input at
-// x = R2 a + b, out(m2, k1, k2, y) receives X[k1 + R1 k2]. All threads of the CTA take part
-// (two barriers).
-template <int NN, int S, class In, class Out>
+// One n-point DFT along the tile's rows for this thread's column, sign S, decomposition D
+// (N = R1 R2 rows, T columns, 256 threads): in(m, b, a) is the input at row R2 a + b,
+// out(m2, k1, k2, y) receives X[k1 + R1 k2]. All threads of the CTA take part (two barriers);
+// mid() runs after the first, when every input has been read.
+template <class D, int S, class In, class Mid, class Out>
 __device__ __forceinline__ void xdft(float2* sm, const float2* tw, int c, int gi, In&& in,
-                                     Out&& out) {
-  using D = XDecomp<NN>;
-  constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
+                                     Mid&& mid, Out&& out) {
+  constexpr int NN = D::N, R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
   constexpr int NB1 = R2 / GR, NB2 = R1 / GR;
 #pragma unroll
   for (int m = 0; m < NB1; m++) {
@@ -171,6 +172,7 @@ __device__ __forceinline__ void xdft(float2* sm, const float2* tw, int c, int gi
     }
   }
   __syncthreads();
+  mid();
 #pragma unroll
   for (int m2 = 0; m2 < NB2; m2++) {
     const int k1 = gi + GR * m2;
@@ -189,7 +191,9 @@ __device__ __forceinline__ void xdft(float2* sm, const float2* tw, int c, int gi
 // so two x transforms give the three components: G_x = F^-1(i w_x u) / N and
 // G_y, G_z = i w_y, i w_z F^-1(u) / N. The inputs of the CTA's next tile are staged into shared
 // memory (cp.async) while the current tile is transformed.
-template <int NN, int MODE>
+// OUT2 (own y / z passes): two arrays out, [G_x, G_0] with G_0 = F^-1(u) / N; otherwise three,
+// [G_x, G_y, G_z].
+template <int NN, int MODE, bool OUT2>
 __global__ void __launch_bounds__(256, 2)
     k_xinv(Geo g, const float* __restrict__ src, float* __restrict__ pdir, float* __restrict__ G3,
            const DevScalars* __restrict__ sc, const float2* __restrict__ tw_g) {
@@ -249,21 +253,29 @@ __global__ void __launch_bounds__(256, 2)
     }
     __syncthreads();  // slots read: stage the next tile behind the transforms
     stage(tile + gridDim.x);
-    xdft<NN, +1>(
+    xdft<D, +1>(
         sm, tw, c, gi,
         [&](int m, int b, int a) {
           const float w = (float)wavenum(R2 * a + b, NN) * invN;
           return make_float2(-w * v[m][a].y, w * v[m][a].x);
         },
-        [&](int, int k1, int k2, float2 y) { Gc[(k1 + R1 * k2) * plane + col.q] = y; });
-    const float fy = (float)col.wy * invN, fz = (float)col.wz * invN;
-    xdft<NN, +1>(
-        sm, tw, c, gi, [&](int m, int, int a) { return v[m][a]; },
-        [&](int, int k1, int k2, float2 y) {
-          const int i = (k1 + R1 * k2) * plane + col.q;
-          Gc[Ns + i] = make_float2(-fy * y.y, fy * y.x);
-          Gc[2 * Ns + i] = make_float2(-fz * y.y, fz * y.x);
-        });
+        [] {}, [&](int, int k1, int k2, float2 y) { Gc[(k1 + R1 * k2) * plane + col.q] = y; });
+    if constexpr (OUT2) {
+      xdft<D, +1>(
+          sm, tw, c, gi, [&](int m, int, int a) { return v[m][a]; }, [] {},
+          [&](int, int k1, int k2, float2 y) {
+            Gc[Ns + (k1 + R1 * k2) * plane + col.q] = make_float2(y.x * invN, y.y * invN);
+          });
+    } else {
+      const float fy = (float)col.wy * invN, fz = (float)col.wz * invN;
+      xdft<D, +1>(
+          sm, tw, c, gi, [&](int m, int, int a) { return v[m][a]; }, [] {},
+          [&](int, int k1, int k2, float2 y) {
+            const int i = (k1 + R1 * k2) * plane + col.q;
+            Gc[Ns + i] = make_float2(-fy * y.y, fy * y.x);
+            Gc[2 * Ns + i] = make_float2(-fz * y.y, fz * y.x);
+          });
+    }
   }
   cp_async_wait<0>();
 }
@@ -271,7 +283,9 @@ __global__ void __launch_bounds__(256, 2)
 // Forward transforms along x of the three spectra F_j of k grad u, the divergence
 // sum_j i w_j F_j = i w_x F(K_x) + F(i w_y K_y + i w_z K_z) (two x transforms), and the epilogue
 // of k_spec_div (same arguments and scalar semantics).
-template <int NN, int EPI>
+// IN2 (own y / z passes): two arrays in, [M_x, M_r] with M_r the spectrum of
+// i w_y K_y + i w_z K_z already transformed along y and z; otherwise three, [K_x, K_y, K_z].
+template <int NN, int EPI, bool IN2>
 __global__ void __launch_bounds__(256, 2)
     k_xfwd(Geo g, const float* __restrict__ G3, const float* __restrict__ aux_in,
            const float* __restrict__ cx, float* __restrict__ out, float* __restrict__ aux_out,
@@ -299,20 +313,26 @@ __global__ void __launch_bounds__(256, 2)
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const XCol col = xcol(g, tile * T + c);
     float2 dsum[NB2][R2];
-    xdft<NN, -1>(
+    xdft<D, -1>(
         sm, tw, c, gi, [&](int, int b, int a1) { return Gc[(R2 * a1 + b) * plane + col.q]; },
+        [] {},
         [&](int m2, int k1, int k2, float2 y) {
           const float w = (float)wavenum(k1 + R1 * k2, NN);
           dsum[m2][k2] = make_float2(-w * y.y, w * y.x);
         });
     const float wy = (float)col.wy, wz = (float)col.wz;
-    xdft<NN, -1>(
+    xdft<D, -1>(
         sm, tw, c, gi,
         [&](int, int b, int a1) {
           const int i = (R2 * a1 + b) * plane + col.q;
-          const float2 gy = Gc[Ns + i], gz = Gc[2 * Ns + i];
-          return make_float2(-(wy * gy.y + wz * gz.y), wy * gy.x + wz * gz.x);
+          if constexpr (IN2) {
+            return Gc[Ns + i];
+          } else {
+            const float2 gy = Gc[Ns + i], gz = Gc[2 * Ns + i];
+            return make_float2(-(wy * gy.y + wz * gz.y), wy * gy.x + wz * gz.x);
+          }
         },
+        [] {},
         [&](int m2, int, int k2, float2 y) {
           dsum[m2][k2].x += y.x;
           dsum[m2][k2].y += y.y;

@@ -236,17 +236,19 @@ def test_repeated_adjoint_after_one_state_solve_checkpointed():
     assert rel_l2(a, f.solve_adjoint(pt)) < 1e-12
 
 
+@pytest.mark.parametrize("path", ["own", "2d"])
 @pytest.mark.parametrize("n", [64, 128, 256])
-def test_xpass_matches_cufft_3d_path(n, monkeypatch):
-    """FP32 D apply, state solve and gradient with the x transform fused into the spectral
-    kernels (k_xinv / k_xfwd around batched 2-D cuFFT) against the 3-D cuFFT path."""
+def test_transform_paths_match_cufft_3d(n, path, monkeypatch):
+    """FP32 D apply, state solve and gradient through the library's own x / y / z transform
+    kernels ("own": k_xinv, k_yinv, k_zpass, k_yfwd, k_xfwd) and through the x pass around
+    batched 2-D cuFFT ("2d"), against the batched 3-D cuFFT path."""
     nt = 3
     wl, tissue, centers = small_problem(n, nt, n_gauss=8)
     d1 = observation(wl, tissue, centers)
     f = reference_test_field(n) + 0.1 * tissue.wm.reshape(-1)
     x = np.concatenate([np.linspace(0.1, 0.9, len(centers)), [wl.kappa, wl.rho]])
     out = []
-    for on in ("1", "0"):
+    for on in (path, "0"):
         monkeypatch.setenv("GLIA_XPASS", on)
         g = gpu(n, MIXED)
         configure(g, wl, tissue, centers)
