@@ -54,27 +54,32 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
 }
 
-// Stages NN rows of T complex (row r at src + r * pitch) as slot[r * T + col], 8-byte copies
-// (the rows of a half-spectrum layout are only 8-byte aligned).
+// Stages the T-column block at column kz0 of NN half-spectrum rows (row r at src + r * nh,
+// 8-byte aligned only: rows start 16-byte aligned when r is even) with 16-byte copies: row r is
+// copied from column kz0 - (r & 1) as (T + 2) complex, so slot[r * (T + 2) + (r & 1) + col]
+// holds column kz0 + col. The copied window stays inside the array or the memory right after it.
 template <int NN, int T>
-__device__ __forceinline__ void stage_rows8(float2* slot, const float2* src, int pitch) {
-  static_assert((NN * T) % 256 == 0, "tile must divide over 256 threads");
+__device__ __forceinline__ void stage_rows_hs(float2* slot, const float2* src, int nh, int kz0) {
+  constexpr int CR = T / 2 + 1, NCH = NN * CR;  // 16-byte chunks per row, per tile
 #pragma unroll
-  for (int j = 0; j < NN * T / 256; j++) {
+  for (int j = 0; j < (NCH + 255) / 256; j++) {
     const int e = (int)threadIdx.x + 256 * j;
-    const int r = e / T, col = e - r * T;
-    cp_async8(slot + r * T + col, src + r * pitch + col);
+    if (NCH % 256 == 0 || e < NCH) {
+      const int r = e / CR, ch = e - r * CR;
+      cp_async16(slot + r * (T + 2) + 2 * ch, src + r * nh + kz0 - (r & 1) + 2 * ch);
+    }
   }
 }
 
 template <int NN>
 constexpr int yinv_smem_bytes() {
-  return (3 * NN * YDecomp<NN>::T + 2 * NN + 256) * (int)sizeof(float2);
+  return (2 * NN * (YDecomp<NN>::T + 2) + NN * YDecomp<NN>::T + 2 * NN + 256) *
+         (int)sizeof(float2);
 }
 
 // G = [G_x, G_0] (half-spectrum layout per x plane) -> H = [H_x, H_y, H_0] (packed lines).
-// Tiles (x, column block of T kz'); G_x and G_0 of the CTA's next tile are staged (cp.async)
-// behind the current tile's transforms.
+// Tiles (x, column block of T kz'); G_x and G_0 of the CTA's next tile are staged (cp.async,
+// 16-byte chunks) behind the current tile's transforms.
 template <int NN>
 __global__ void __launch_bounds__(256, 2)
     k_yinv(const float* __restrict__ Gin, float* __restrict__ Hout,
@@ -83,11 +88,11 @@ __global__ void __launch_bounds__(256, 2)
   constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T, NB1 = R2 / GR;
   constexpr int NQ = NN / 2, NH = NN / 2 + 1, CB = NQ / T;
   constexpr int PS = NN * NH, NS = NN * PS, NP = NN * NN * NQ;
-  constexpr int ntiles = NN * CB;
+  constexpr int ntiles = NN * CB, TS = T + 2;
   extern __shared__ float4 yinv_dyn[];
   float2* slGx = reinterpret_cast<float2*>(yinv_dyn);
-  float2* slG0 = slGx + NN * T;
-  float2* nyq = slG0 + NN * T;  // kz = n/2 columns: [0, NN) of G_x, [NN, 2 NN) of G_0
+  float2* slG0 = slGx + NN * TS;
+  float2* nyq = slG0 + NN * TS;  // kz = n/2 columns: [0, NN) of G_x, [NN, 2 NN) of G_0
   float2* sm = nyq + 2 * NN;
   float2* tw = sm + NN * T;
   for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw_g[i];
@@ -98,7 +103,7 @@ __global__ void __launch_bounds__(256, 2)
   auto stage = [&](float2* slot, float2* ny, const float2* G, int t) {
     if (t < ntiles) {
       const int x = t / CB, cb = t - x * CB;
-      stage_rows8<NN, T>(slot, G + x * PS + cb * T, NH);
+      stage_rows_hs<NN, T>(slot, G + x * PS, NH, cb * T);
       if (cb == 0 && (int)threadIdx.x < NN)
         cp_async8(ny + threadIdx.x, G + x * PS + (int)threadIdx.x * NH + NQ);
     }
@@ -115,7 +120,7 @@ __global__ void __launch_bounds__(256, 2)
         sm, tw, c, gi,
         [&](int, int b, int a) {
           const int ky = R2 * a + b;
-          float2 v = slGx[ky * T + c];
+          float2 v = slGx[ky * TS + (ky & 1) + c];
           if (pk) {
             const float2 w = nyq[ky];
             v = make_float2(v.x - w.y, v.y + w.x);
@@ -133,7 +138,7 @@ __global__ void __launch_bounds__(256, 2)
 #pragma unroll
       for (int a = 0; a < R1; a++) {
         const int ky = R2 * a + b;
-        float2 val = slG0[ky * T + c];
+        float2 val = slG0[ky * TS + (ky & 1) + c];
         if (pk) {
           const float2 w = nyq[NN + ky];
           val = make_float2(val.x - w.y, val.y + w.x);
@@ -257,7 +262,7 @@ struct ZGeom {
 
 template <int NN>
 constexpr int zpass_smem_bytes() {
-  return (3 * ZGeom<NN>::SLOT + 256) * (int)sizeof(float2);
+  return (3 * ZGeom<NN>::SLOT + 256 + NN) * (int)sizeof(float2);
 }
 
 // Stages LB contiguous lines of NQ complex (or of n floats) into a slot of line stride LS.
@@ -291,7 +296,17 @@ __global__ void __launch_bounds__(256, 2)
   extern __shared__ float4 zpass_dyn[];
   float2* slots = reinterpret_cast<float2*>(zpass_dyn);
   float2* tw = slots + 3 * Z::SLOT;
+  // per-stage twiddles in the order the threads of a line read them (conflict-free):
+  // twA[k1 R2 + t] = exp(+2 pi i t k1 / (n/2)), twB[k2 R1 + m1] = exp(-2 pi i m1 k2 / (n/2))
+  float2* twA = tw + 256;
+  float2* twB = twA + NQ;
   for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw_g[i];
+  for (int i = threadIdx.x; i < NQ; i += blockDim.x) {
+    const int k1 = i / R2, tt = i - k1 * R2;
+    twA[i] = tw_n<NQ, +1>(tw_g, tt * k1);
+    const int k2 = i / R1, m1 = i - k2 * R1;
+    twB[i] = tw_n<NQ, -1>(tw_g, m1 * k2);
+  }
   const int l = threadIdx.x / R2, t = threadIdx.x % R2;
   float2* Hc = reinterpret_cast<float2*>(Hio);
   const int nblk = (int)blockIdx.x < Z::NBLK
@@ -354,7 +369,7 @@ __global__ void __launch_bounds__(256, 2)
     reg_dft<R1, +1>(u);
 #pragma unroll
     for (int k1 = 0; k1 < R1; k1++) {
-      if (k1) u[k1] = cmul2(u[k1], tw_n<NQ, +1>(tw, t * k1));
+      if (k1) u[k1] = cmul2(u[k1], twA[k1 * R2 + t]);
       S[k1 * R2 + (t ^ (k1 & (R2 - 1)))] = u[k1];
     }
     __syncthreads();
@@ -371,7 +386,7 @@ __global__ void __launch_bounds__(256, 2)
       reg_dft<R2, -1>(z[ii]);  // forward, first stage: over m2 for m1 = k1
 #pragma unroll
       for (int k2 = 1; k2 < R2; k2++)
-        if (k1) z[ii][k2] = cmul2(z[ii][k2], tw_n<NQ, -1>(tw, k1 * k2));
+        if (k1) z[ii][k2] = cmul2(z[ii][k2], twB[k2 * R1 + k1]);
     }
     __syncthreads();
 #pragma unroll

@@ -42,52 +42,94 @@ __device__ __forceinline__ float2 cmul2(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-// exp(-2 pi i j / 16), j in [0, 16)
-__device__ __forceinline__ float2 w16(int j) {
-  constexpr float c[16] = {1.000000000f,  0.923879533f,  0.707106781f,  0.382683432f,
-                           0.000000000f,  -0.382683432f, -0.707106781f, -0.923879533f,
-                           -1.000000000f, -0.923879533f, -0.707106781f, -0.382683432f,
-                           0.000000000f,  0.382683432f,  0.707106781f,  0.923879533f};
-  constexpr float s[16] = {0.000000000f,  -0.382683432f, -0.707106781f, -0.923879533f,
-                           -1.000000000f, -0.923879533f, -0.707106781f, -0.382683432f,
-                           0.000000000f,  0.382683432f,  0.707106781f,  0.923879533f,
-                           1.000000000f,  0.923879533f,  0.707106781f,  0.382683432f};
-  return make_float2(c[j & 15], s[j & 15]);
+// In-register DFTs, natural order in and out: X[k] = sum_j v[j] exp(S 2 pi i j k / R) for
+// R = 2, 4, 8, 16, built from radix-4 butterflies (the factors +-i and -1 are sign changes and
+// swaps, never multiplications).
+template <int S>
+__device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2& a3) {
+  const float2 t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3), t3 = csub(a1, a3);
+  a0 = cadd(t0, t2);
+  a2 = csub(t0, t2);
+  a1 = make_float2(t1.x - S * t3.y, t1.y + S * t3.x);  // t1 + S i t3
+  a3 = make_float2(t1.x + S * t3.y, t1.y - S * t3.x);  // t1 - S i t3
 }
 
-__host__ __device__ constexpr int brev_bits(int i, int bits) {
-  int r = 0;
-  for (int b = 0; b < bits; b++)
-    if (i & (1 << b)) r |= 1 << (bits - 1 - b);
-  return r;
+// exp(S 2 pi i e / 16) times z for a compile-time e; e = 4 is S i (a swap)
+template <int S, int E>
+__device__ __forceinline__ float2 tw16(float2 z) {
+  constexpr int e = E & 15;
+  if constexpr (e == 0) {
+    return z;
+  } else if constexpr (e == 4) {
+    return make_float2(-S * z.y, S * z.x);
+  } else if constexpr (e == 8) {
+    return make_float2(-z.x, -z.y);
+  } else if constexpr (e == 12) {
+    return make_float2(S * z.y, -S * z.x);
+  } else {
+    constexpr float c[16] = {1.000000000f,  0.923879533f,  0.707106781f,  0.382683432f,
+                             0.000000000f,  -0.382683432f, -0.707106781f, -0.923879533f,
+                             -1.000000000f, -0.923879533f, -0.707106781f, -0.382683432f,
+                             0.000000000f,  0.382683432f,  0.707106781f,  0.923879533f};
+    const float wc = c[e], ws = S * c[(e + 12) & 15];  // sin(2 pi e / 16) = cos(2 pi (e - 4) / 16)
+    return make_float2(z.x * wc - z.y * ws, z.x * ws + z.y * wc);
+  }
 }
 
-// In-register DFT of size R (2, 4, 8 or 16): X[k] = sum_i v[i] exp(S 2 pi i i k / R), natural
-// order in and out (iterative radix-2 on the bit-reversed copy).
 template <int R, int S>
 __device__ __forceinline__ void reg_dft(float2 (&v)[R]) {
   static_assert(R == 2 || R == 4 || R == 8 || R == 16, "register DFT sizes 2 ... 16");
-  constexpr int LOG = R == 16 ? 4 : (R == 8 ? 3 : (R == 4 ? 2 : 1));
-  float2 t[R];
+  if constexpr (R == 2) {
+    const float2 a = v[0];
+    v[0] = cadd(a, v[1]);
+    v[1] = csub(a, v[1]);
+  } else if constexpr (R == 4) {
+    dft4<S>(v[0], v[1], v[2], v[3]);
+  } else if constexpr (R == 8) {
+    // decimation in time: X[k] = E[k] + W^k O[k], X[k + 4] = E[k] - W^k O[k], W = w_16^2
+    float2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    float2 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4<S>(e0, e1, e2, e3);
+    dft4<S>(o0, o1, o2, o3);
+    o1 = tw16<S, 2>(o1);
+    o2 = tw16<S, 4>(o2);
+    o3 = tw16<S, 6>(o3);
+    v[0] = cadd(e0, o0);
+    v[4] = csub(e0, o0);
+    v[1] = cadd(e1, o1);
+    v[5] = csub(e1, o1);
+    v[2] = cadd(e2, o2);
+    v[6] = csub(e2, o2);
+    v[3] = cadd(e3, o3);
+    v[7] = csub(e3, o3);
+  } else {
+    // 4 x 4: j = 4 j1 + j2; DFT over j1, twiddle w_16^(j2 k1), DFT over j2; k = k1 + 4 k2
+    dft4<S>(v[0], v[4], v[8], v[12]);
+    dft4<S>(v[1], v[5], v[9], v[13]);
+    dft4<S>(v[2], v[6], v[10], v[14]);
+    dft4<S>(v[3], v[7], v[11], v[15]);
+    v[5] = tw16<S, 1>(v[5]);
+    v[6] = tw16<S, 2>(v[6]);
+    v[7] = tw16<S, 3>(v[7]);
+    v[9] = tw16<S, 2>(v[9]);
+    v[10] = tw16<S, 4>(v[10]);
+    v[11] = tw16<S, 6>(v[11]);
+    v[13] = tw16<S, 3>(v[13]);
+    v[14] = tw16<S, 6>(v[14]);
+    v[15] = tw16<S, 9>(v[15]);
+    dft4<S>(v[0], v[1], v[2], v[3]);
+    dft4<S>(v[4], v[5], v[6], v[7]);
+    dft4<S>(v[8], v[9], v[10], v[11]);
+    dft4<S>(v[12], v[13], v[14], v[15]);
+    // v[4 k1 + k2] holds X[k1 + 4 k2]: transpose to natural order
+    float2 t[16];
 #pragma unroll
-  for (int i = 0; i < R; i++) t[brev_bits(i, LOG)] = v[i];
+    for (int k1 = 0; k1 < 4; k1++)
 #pragma unroll
-  for (int len = 2; len <= R; len <<= 1) {
+      for (int k2 = 0; k2 < 4; k2++) t[k1 + 4 * k2] = v[4 * k1 + k2];
 #pragma unroll
-    for (int i = 0; i < R; i += len) {
-#pragma unroll
-      for (int j = 0; j < len / 2; j++) {
-        float2 w = w16(j * (16 / len));
-        if (S > 0) w.y = -w.y;
-        const float2 u = t[i + j];
-        const float2 x = cmul2(t[i + j + len / 2], w);
-        t[i + j] = cadd(u, x);
-        t[i + j + len / 2] = csub(u, x);
-      }
-    }
+    for (int i = 0; i < 16; i++) v[i] = t[i];
   }
-#pragma unroll
-  for (int i = 0; i < R; i++) v[i] = t[i];
 }
 
 // twiddle exp(S 2 pi i e / n) from the shared table W_256^j = exp(-2 pi i j / 256)
@@ -259,7 +301,8 @@ __global__ void __launch_bounds__(256, 2)
           const float w = (float)wavenum(R2 * a + b, NN) * invN;
           return make_float2(-w * v[m][a].y, w * v[m][a].x);
         },
-        [] {}, [&](int, int k1, int k2, float2 y) { Gc[(k1 + R1 * k2) * plane + col.q] = y; });
+        [] {},
+        [&](int, int k1, int k2, float2 y) { Gc[(k1 + R1 * k2) * plane + col.q] = y; });
     if constexpr (OUT2) {
       xdft<D, +1>(
           sm, tw, c, gi, [&](int m, int, int a) { return v[m][a]; }, [] {},
