@@ -428,9 +428,14 @@ class Engine final : public EngineBase {
   }
   template <int NN, int EPI, bool IN2>
   void xfwd_n(const R* G, const R* aux_in, const R* cx, R* out, R* aux_out, R scale, int blocks) {
-    if constexpr (std::is_same<R, float>::value)
-      k_xfwd<NN, EPI, IN2><<<blocks, 256, 0, stream_>>>(g_, G, aux_in, cx, out, aux_out, scale,
-                                                         sc_, ws_, tw256_);
+    if constexpr (std::is_same<R, float>::value) {
+      if constexpr (IN2)
+        k_xfwd_own<NN, EPI><<<blocks, 256, xfwd_own_smem_bytes<NN>(), stream_>>>(
+            g_, G, aux_in, cx, out, aux_out, scale, sc_, ws_, tw256_);
+      else
+        k_xfwd<NN, EPI><<<blocks, 256, 0, stream_>>>(g_, G, aux_in, cx, out, aux_out, scale, sc_,
+                                                     ws_, tw256_);
+    }
   }
   template <int EPI>
   void launch_xfwd(const R* aux_in, const R* cx, R* out, R* aux_out, R scale, int blocks) {
@@ -458,7 +463,8 @@ class Engine final : public EngineBase {
         k_zpass<NN><<<std::min(own_res_[1], pw_blocks_), 256, zpass_smem_bytes<NN>(), stream_>>>(
             g3s_, kxx_, tw256_);
       else
-        k_yfwd<NN><<<std::min(own_res_[2], pw_blocks_), 256, 0, stream_>>>(g3s_, g3r_, tw256_);
+        k_yfwd<NN><<<std::min(own_res_[2], pw_blocks_), 256, yfwd_smem_bytes<NN>(), stream_>>>(
+            g3s_, g3r_, tw256_);
     }
   }
   void launch_own(int which) {
@@ -482,18 +488,19 @@ class Engine final : public EngineBase {
       if (own_) {
         xres_inv_ = sms_ * std::min(per_sm(k_xinv<NN, 0, true>, xinv_smem_bytes<NN, 0>()),
                                     per_sm(k_xinv<NN, 1, true>, xinv_smem_bytes<NN, 1>()));
-        xres_fwd_ = sms_ * std::min({per_sm(k_xfwd<NN, EPI_APPLYD, true>, 0),
-                                     per_sm(k_xfwd<NN, EPI_SETUP, true>, 0),
-                                     per_sm(k_xfwd<NN, EPI_CGW, true>, 0)});
+        constexpr int fs = xfwd_own_smem_bytes<NN>();
+        xres_fwd_ = sms_ * std::min({per_sm(k_xfwd_own<NN, EPI_APPLYD>, fs),
+                                     per_sm(k_xfwd_own<NN, EPI_SETUP>, fs),
+                                     per_sm(k_xfwd_own<NN, EPI_CGW>, fs)});
         own_res_[0] = sms_ * per_sm(k_yinv<NN>, yinv_smem_bytes<NN>());
         own_res_[1] = sms_ * per_sm(k_zpass<NN>, zpass_smem_bytes<NN>());
-        own_res_[2] = sms_ * per_sm(k_yfwd<NN>, 0);
+        own_res_[2] = sms_ * per_sm(k_yfwd<NN>, yfwd_smem_bytes<NN>());
       } else {
         xres_inv_ = sms_ * std::min(per_sm(k_xinv<NN, 0, false>, xinv_smem_bytes<NN, 0>()),
                                     per_sm(k_xinv<NN, 1, false>, xinv_smem_bytes<NN, 1>()));
-        xres_fwd_ = sms_ * std::min({per_sm(k_xfwd<NN, EPI_APPLYD, false>, 0),
-                                     per_sm(k_xfwd<NN, EPI_SETUP, false>, 0),
-                                     per_sm(k_xfwd<NN, EPI_CGW, false>, 0)});
+        xres_fwd_ = sms_ * std::min({per_sm(k_xfwd<NN, EPI_APPLYD>, 0),
+                                     per_sm(k_xfwd<NN, EPI_SETUP>, 0),
+                                     per_sm(k_xfwd<NN, EPI_CGW>, 0)});
       }
     }
   }

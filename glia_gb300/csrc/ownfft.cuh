@@ -162,7 +162,15 @@ __global__ void __launch_bounds__(256, 2)
   cp_async_wait<0>();
 }
 
+template <int NN>
+constexpr int yfwd_smem_bytes() {
+  return (3 * NN * YDecomp<NN>::T + 2 * NN + 256) * (int)sizeof(float2);
+}
+
 // K = [K_x, K_y, L_z] (packed lines) -> M = [M_x, M_r] (half-spectrum layout per x plane).
+// The CTA's inputs form a stream of items (K_x, K_y, L_z of its first tile, then of the next,
+// ...) through two shared-memory slots: item i sits in slot i % 2 and, once the transform that
+// reads it has its inputs in registers, item i + 2 is staged there (cp.async).
 template <int NN>
 __global__ void __launch_bounds__(256, 2)
     k_yfwd(const float* __restrict__ Kin, float* __restrict__ Mout,
@@ -172,49 +180,82 @@ __global__ void __launch_bounds__(256, 2)
   constexpr int NQ = NN / 2, NH = NN / 2 + 1, CB = NQ / T;
   constexpr int PS = NN * NH, NS = NN * PS, NP = NN * NN * NQ;
   constexpr int ntiles = NN * CB;
-  __shared__ float2 sm[NN * T];
-  __shared__ float2 zA[NN], zB[NN];
-  __shared__ float2 tw[256];
+  extern __shared__ float4 yfwd_dyn[];
+  float2* slots = reinterpret_cast<float2*>(yfwd_dyn);  // 2 x NN * T
+  float2* sm = slots + 2 * NN * T;
+  float2* zA = sm + NN * T;
+  float2* zB = zA + NN;
+  float2* tw = zB + NN;
   for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw_g[i];
   const int c = threadIdx.x % T, gi = threadIdx.x / T;
-  const float2* Kx = reinterpret_cast<const float2*>(Kin);
-  const float2* Ky = Kx + NP;
-  const float2* Lz = Kx + 2 * NP;
+  const float2* K = reinterpret_cast<const float2*>(Kin);
   float2* Mx = reinterpret_cast<float2*>(Mout);
   float2* Mr = Mx + NS;
-  __syncthreads();
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  const int mytiles =
+      (int)blockIdx.x < ntiles ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
+                               : 0;
+  const int nitems = 3 * mytiles;
+  auto issue = [&](int i) {
+    if (i < nitems) {
+      const int t = (int)blockIdx.x + (i / 3) * (int)gridDim.x, j = i % 3;
+      const int x = t / CB, cb = t - x * CB;
+      stage_tile<NN, T>(slots + (i & 1) * NN * T, K + (size_t)j * NP + (size_t)x * NN * NQ, NQ, cb);
+    }
+    cp_async_commit();
+  };
+  issue(0);
+  issue(1);
+  for (int it = 0; it < mytiles; it++) {
+    const int tile = (int)blockIdx.x + it * (int)gridDim.x;
     const int x = tile / CB, cb = tile - x * CB, kz = cb * T + c;
     const bool pk = kz == 0;
-    const int row0 = x * NN;
-    xdft<D, -1>(
-        sm, tw, c, gi, [&](int, int b, int a) { return Kx[(row0 + R2 * a + b) * NQ + kz]; }, [] {},
-        [&](int, int k1, int k2, float2 y) {
-          const int ky = k1 + R1 * k2;
-          if (pk)
-            zA[ky] = y;
-          else
-            Mx[x * PS + ky * NH + kz] = y;
-        });
+    const int i0 = 3 * it;
+    auto slot = [&](int i) { return slots + (i & 1) * NN * T; };
+    cp_async_wait<1>();
+    __syncthreads();
+    {
+      const float2* S = slot(i0);
+      xdft<D, -1>(
+          sm, tw, c, gi, [&](int, int b, int a) { return S[(R2 * a + b) * T + c]; },
+          [&] { issue(i0 + 2); },
+          [&](int, int k1, int k2, float2 y) {
+            const int ky = k1 + R1 * k2;
+            if (pk)
+              zA[ky] = y;
+            else
+              Mx[x * PS + ky * NH + kz] = y;
+          });
+    }
     float2 dsum[NB2][R2];
-    xdft<D, -1>(
-        sm, tw, c, gi, [&](int, int b, int a) { return Ky[(row0 + R2 * a + b) * NQ + kz]; }, [] {},
-        [&](int m2, int k1, int k2, float2 y) {
-          const float w = (float)wavenum(k1 + R1 * k2, NN);
-          dsum[m2][k2] = make_float2(-w * y.y, w * y.x);
-        });
-    xdft<D, -1>(
-        sm, tw, c, gi, [&](int, int b, int a) { return Lz[(row0 + R2 * a + b) * NQ + kz]; }, [] {},
-        [&](int m2, int k1, int k2, float2 y) {
-          const int ky = k1 + R1 * k2;
-          const float2 d = make_float2(dsum[m2][k2].x + y.x, dsum[m2][k2].y + y.y);
-          if (pk)
-            zB[ky] = d;
-          else
-            Mr[x * PS + ky * NH + kz] = d;
-        });
+    cp_async_wait<1>();
+    __syncthreads();
+    {
+      const float2* S = slot(i0 + 1);
+      xdft<D, -1>(
+          sm, tw, c, gi, [&](int, int b, int a) { return S[(R2 * a + b) * T + c]; },
+          [&] { issue(i0 + 3); },
+          [&](int m2, int k1, int k2, float2 y) {
+            const float w = (float)wavenum(k1 + R1 * k2, NN);
+            dsum[m2][k2] = make_float2(-w * y.y, w * y.x);
+          });
+    }
+    cp_async_wait<1>();
+    __syncthreads();
+    {
+      const float2* S = slot(i0 + 2);
+      xdft<D, -1>(
+          sm, tw, c, gi, [&](int, int b, int a) { return S[(R2 * a + b) * T + c]; },
+          [&] { issue(i0 + 4); },
+          [&](int m2, int k1, int k2, float2 y) {
+            const int ky = k1 + R1 * k2;
+            const float2 d = make_float2(dsum[m2][k2].x + y.x, dsum[m2][k2].y + y.y);
+            if (pk)
+              zB[ky] = d;
+            else
+              Mr[x * PS + ky * NH + kz] = d;
+          });
+    }
     if (cb == 0) {  // unpack the kz' = 0 column into kz = 0 and kz = n/2
-      __syncthreads();
       if (c == 0) {
         for (int ky = gi; ky < NN; ky += GR) {
           const int km = (NN - ky) & (NN - 1);
@@ -222,16 +263,17 @@ __global__ void __launch_bounds__(256, 2)
           for (int h = 0; h < 2; h++) {
             const float2 z = h ? zB[ky] : zA[ky];
             const float2 zm = h ? zB[km] : zA[km];
-            const float2 s = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
-            const float2 d = make_float2(0.5f * (z.y + zm.y), -0.5f * (z.x - zm.x));
+            const float2 s2 = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
+            const float2 d2 = make_float2(0.5f * (z.y + zm.y), -0.5f * (z.x - zm.x));
             float2* M = h ? Mr : Mx;
-            M[x * PS + ky * NH] = s;
-            M[x * PS + ky * NH + NQ] = d;
+            M[x * PS + ky * NH] = s2;
+            M[x * PS + ky * NH + NQ] = d2;
           }
         }
       }
     }
   }
+  cp_async_wait<0>();
 }
 
 // z transforms: n/2 = R1 R2 complex points per line, R2 threads per line, 256 / R2 lines per

@@ -323,12 +323,52 @@ __global__ void __launch_bounds__(256, 2)
   cp_async_wait<0>();
 }
 
-// Forward transforms along x of the three spectra F_j of k grad u, the divergence
-// sum_j i w_j F_j = i w_x F(K_x) + F(i w_y K_y + i w_z K_z) (two x transforms), and the epilogue
-// of k_spec_div (same arguments and scalar semantics).
-// IN2 (own y / z passes): two arrays in, [M_x, M_r] with M_r the spectrum of
-// i w_y K_y + i w_z K_z already transformed along y and z; otherwise three, [K_x, K_y, K_z].
-template <int NN, int EPI, bool IN2>
+// Epilogue of the forward x pass for one output element (k_spec_div semantics): d = the
+// divergence sum_j i w_j F_j at (kx, column), av = the CG direction (CGW) or the spectrum of c
+// (SETUP), xv = the spectrum of the caller's x (SETUP with cx).
+template <int NN, int EPI>
+__device__ __forceinline__ void xfwd_epilogue(float2 d, int kx, int idx, const XCol& col, float a,
+                                              float pcc, float invN, float scale, float2 av,
+                                              float2 xv, bool has_cx, float2* O, float2* AO,
+                                              Acc<float> (&acc)[4]) {
+  if (EPI == EPI_APPLYD) {
+    O[idx] = make_float2(d.x * scale, d.y * scale);
+  } else if (EPI == EPI_SETUP) {
+    const float br = av.x + a * d.x, bi = av.y + a * d.y;
+    const float rr = 2.f * a * d.x, ri = 2.f * a * d.y;
+    const float pm = pc_mult<float>(pcc, wavenum(kx, NN), col.wy, col.wz);
+    const float r2 = rr * rr + ri * ri;
+    acc[0].add(col.mult * pm * pm * (br * br + bi * bi));
+    acc[1].add(col.mult * pm * pm * r2);
+    acc[2].add(col.mult * pm * r2);
+    if (has_cx) acc[3].add(col.mult * (xv.x * d.x + xv.y * d.y));
+    O[idx] = make_float2(av.x * invN, av.y * invN);
+    AO[idx] = make_float2(rr, ri);
+  } else {  // EPI_CGW
+    const float wr = av.x - a * d.x, wi = av.y - a * d.y;
+    acc[0].add(col.mult * (av.x * wr + av.y * wi));
+    O[idx] = make_float2(wr, wi);
+  }
+}
+
+template <int EPI>
+__device__ __forceinline__ void xfwd_finish(Acc<float> (&acc)[4], Geo g, DevScalars* sc, RedWs ws,
+                                            bool has_cx) {
+  if constexpr (EPI == EPI_SETUP) {
+    double sums[4] = {acc[0].value(), acc[1].value(), acc[2].value(), acc[3].value()};
+    if (!grid_sum_last<4>(sums, ws)) return;
+    if (threadIdx.x == 0) div_setup_finish(sums, sc, g.invN, has_cx);
+  } else if constexpr (EPI == EPI_CGW) {
+    double sums[1] = {acc[0].value()};
+    if (!grid_sum_last<1>(sums, ws)) return;
+    if (threadIdx.x == 0) div_cgw_finish(sums[0], sc, g.invN);
+  }
+}
+
+// Forward transforms along x of the three spectra F_j of k grad u (the cuFFT 2-D path: layout
+// (x, ky, kz) per component), the divergence sum_j i w_j F_j = i w_x F(K_x) +
+// F(i w_y K_y + i w_z K_z) (two x transforms), and the epilogue of k_spec_div.
+template <int NN, int EPI>
 __global__ void __launch_bounds__(256, 2)
     k_xfwd(Geo g, const float* __restrict__ G3, const float* __restrict__ aux_in,
            const float* __restrict__ cx, float* __restrict__ out, float* __restrict__ aux_out,
@@ -368,12 +408,8 @@ __global__ void __launch_bounds__(256, 2)
         sm, tw, c, gi,
         [&](int, int b, int a1) {
           const int i = (R2 * a1 + b) * plane + col.q;
-          if constexpr (IN2) {
-            return Gc[Ns + i];
-          } else {
-            const float2 gy = Gc[Ns + i], gz = Gc[2 * Ns + i];
-            return make_float2(-(wy * gy.y + wz * gz.y), wy * gy.x + wz * gz.x);
-          }
+          const float2 gy = Gc[Ns + i], gz = Gc[2 * Ns + i];
+          return make_float2(-(wy * gy.y + wz * gz.y), wy * gy.x + wz * gz.x);
         },
         [] {},
         [&](int m2, int, int k2, float2 y) {
@@ -387,42 +423,127 @@ __global__ void __launch_bounds__(256, 2)
       for (int k2 = 0; k2 < R2; k2++) {
         const int kx = k1 + R1 * k2;
         const int idx = kx * plane + col.q;
-        const float2 d = dsum[m2][k2];
-        if (EPI == EPI_APPLYD) {
-          O[idx] = make_float2(d.x * scale, d.y * scale);
-        } else if (EPI == EPI_SETUP) {
-          const float2 cv = AX[idx];
-          const float br = cv.x + a * d.x, bi = cv.y + a * d.y;
-          const float rr = 2.f * a * d.x, ri = 2.f * a * d.y;
-          const float pm = pc_mult<float>(pcc, wavenum(kx, NN), col.wy, col.wz);
-          const float r2 = rr * rr + ri * ri;
-          acc[0].add(col.mult * pm * pm * (br * br + bi * bi));
-          acc[1].add(col.mult * pm * pm * r2);
-          acc[2].add(col.mult * pm * r2);
-          if (CX) {
-            const float2 xv = CX[idx];
-            acc[3].add(col.mult * (xv.x * d.x + xv.y * d.y));
-          }
-          O[idx] = make_float2(cv.x * invN, cv.y * invN);
-          AO[idx] = make_float2(rr, ri);
-        } else {  // EPI_CGW
-          const float2 p = AX[idx];
-          const float wr = p.x - a * d.x, wi = p.y - a * d.y;
-          acc[0].add(col.mult * (p.x * wr + p.y * wi));
-          O[idx] = make_float2(wr, wi);
-        }
+        const float2 av = EPI == EPI_APPLYD ? make_float2(0.f, 0.f) : AX[idx];
+        const float2 xv = (EPI == EPI_SETUP && CX) ? CX[idx] : make_float2(0.f, 0.f);
+        xfwd_epilogue<NN, EPI>(dsum[m2][k2], kx, idx, col, a, pcc, invN, scale, av, xv,
+                               CX != nullptr, O, AO, acc);
       }
     }
   }
-  if constexpr (EPI == EPI_SETUP) {
-    double sums[4] = {acc[0].value(), acc[1].value(), acc[2].value(), acc[3].value()};
-    if (!grid_sum_last<4>(sums, ws)) return;
-    if (threadIdx.x == 0) div_setup_finish(sums, sc, g.invN, cx != nullptr);
-  } else if constexpr (EPI == EPI_CGW) {
-    double sums[1] = {acc[0].value()};
-    if (!grid_sum_last<1>(sums, ws)) return;
-    if (threadIdx.x == 0) div_cgw_finish(sums[0], sc, g.invN);
+  xfwd_finish<EPI>(acc, g, sc, ws, cx != nullptr);
+}
+
+template <int NN>
+constexpr int xfwd_own_smem_bytes() {
+  return (3 * NN * XDecomp<NN>::T + 256) * (int)sizeof(float2);
+}
+
+// Forward x pass of the own-transform path: M = [M_x, M_r] in the half-spectrum layout,
+// divergence i w_x F_x M_x + F_x M_r, epilogue of k_spec_div. The CTA's inputs form a stream of
+// items (M_x, M_r and the epilogue's spectra of its first tile, then of the next, ...) through
+// two shared-memory slots: item i sits in slot i % 2 and, once consumed, its slot receives item
+// i + 2 (cp.async).
+template <int NN, int EPI>
+__global__ void __launch_bounds__(256, 2)
+    k_xfwd_own(Geo g, const float* __restrict__ M2, const float* __restrict__ aux_in,
+               const float* __restrict__ cx, float* __restrict__ out, float* __restrict__ aux_out,
+               float scale, DevScalars* __restrict__ sc, RedWs ws,
+               const float2* __restrict__ tw_g) {
+  using D = XDecomp<NN>;
+  constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
+  constexpr int NB2 = R1 / GR;
+  extern __shared__ float4 xfwd_dyn[];
+  float2* slots = reinterpret_cast<float2*>(xfwd_dyn);  // 2 x NN * T
+  float2* sm = slots + 2 * NN * T;
+  float2* tw = sm + NN * T;
+  if (EPI == EPI_CGW && sc->status != 0) return;
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw_g[i];
+  const int c = threadIdx.x % T, gi = threadIdx.x / T;
+  const int plane = NN * g.nh, Ns = plane * NN;
+  const int ntiles = plane / T;
+  const float a = EPI == EPI_APPLYD ? 0.f : (float)sc->a_cn;
+  const float pcc = (float)sc->pc_c;
+  const float invN = (float)g.invN;
+  const float2* Mx = reinterpret_cast<const float2*>(M2);
+  const float2* Mr = Mx + Ns;
+  const float2* AX = reinterpret_cast<const float2*>(aux_in);
+  const float2* CX = reinterpret_cast<const float2*>(cx);
+  float2* O = reinterpret_cast<float2*>(out);
+  float2* AO = reinterpret_cast<float2*>(aux_out);
+  const int naux = EPI == EPI_APPLYD ? 0 : (EPI == EPI_SETUP && CX ? 2 : 1);
+  const int NI = 2 + naux;
+  const int mytiles =
+      (int)blockIdx.x < ntiles ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
+                               : 0;
+  const int nitems = NI * mytiles;
+  auto slot = [&](int i) { return slots + (i & 1) * NN * T; };
+  auto issue = [&](int i) {
+    if (i < nitems) {
+      const int t = (int)blockIdx.x + (i / NI) * (int)gridDim.x, kind = i % NI;
+      const float2* src = kind == 0 ? Mx : (kind == 1 ? Mr : (kind == 2 ? AX : CX));
+      stage_tile<NN, T>(slot(i), src, plane, t);
+    }
+    cp_async_commit();
+  };
+  issue(0);
+  issue(1);
+  Acc<float> acc[4];
+  for (int it = 0; it < mytiles; it++) {
+    const int tile = (int)blockIdx.x + it * (int)gridDim.x;
+    const int i0 = NI * it;
+    const XCol col = xcol(g, tile * T + c);
+    float2 dsum[NB2][R2];
+    cp_async_wait<1>();
+    __syncthreads();
+    {
+      const float2* S = slot(i0);
+      xdft<D, -1>(
+          sm, tw, c, gi, [&](int, int b, int a1) { return S[(R2 * a1 + b) * T + c]; },
+          [&] { issue(i0 + 2); },
+          [&](int m2, int k1, int k2, float2 y) {
+            const float w = (float)wavenum(k1 + R1 * k2, NN);
+            dsum[m2][k2] = make_float2(-w * y.y, w * y.x);
+          });
+    }
+    cp_async_wait<1>();
+    __syncthreads();
+    {
+      const float2* S = slot(i0 + 1);
+      xdft<D, -1>(
+          sm, tw, c, gi, [&](int, int b, int a1) { return S[(R2 * a1 + b) * T + c]; },
+          [&] { issue(i0 + 3); },
+          [&](int m2, int, int k2, float2 y) {
+            dsum[m2][k2].x += y.x;
+            dsum[m2][k2].y += y.y;
+          });
+    }
+    if (naux == 2)
+      cp_async_wait<0>();
+    else
+      cp_async_wait<1>();
+    __syncthreads();
+    const float2* SA = slot(i0 + 2);
+    const float2* SX = slot(i0 + 3);
+#pragma unroll
+    for (int m2 = 0; m2 < NB2; m2++) {
+      const int k1 = gi + GR * m2;
+#pragma unroll
+      for (int k2 = 0; k2 < R2; k2++) {
+        const int kx = k1 + R1 * k2;
+        const float2 av = naux ? SA[kx * T + c] : make_float2(0.f, 0.f);
+        const float2 xv = naux == 2 ? SX[kx * T + c] : make_float2(0.f, 0.f);
+        xfwd_epilogue<NN, EPI>(dsum[m2][k2], kx, kx * plane + col.q, col, a, pcc, invN, scale, av,
+                               xv, naux == 2, O, AO, acc);
+      }
+    }
+    if (naux) {
+      __syncthreads();  // the epilogue's slots are read: stage the next tile's M_x (and M_r)
+      issue(i0 + 4);
+      if (naux == 2) issue(i0 + 5);
+    }
   }
+  cp_async_wait<0>();
+  xfwd_finish<EPI>(acc, g, sc, ws, naux == 2);
 }
 
 }  // namespace glia
