@@ -323,7 +323,10 @@ def run_ours(args, torch, api, wl, tissue, centers, stream, ws, rank):
     if not args.timing_off:
         ctx.set_timing(True)
         flush.fill_(1.0)
+        torch.cuda.nvtx.range_push("instrumented_eval")
         ctx.eval_objective_and_gradient(x, d_dev)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         kt = ctx.timing()
         ctx.set_timing(False)
 
