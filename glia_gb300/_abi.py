@@ -121,6 +121,7 @@ SIGNATURES = {
     "eval_objective": (c_int, [_CTX, _D, c_int, _P, _D]),
     "eval_gradient": (c_int, [_CTX, _D, c_int, _P, _D]),
     "eval_objective_and_gradient": (c_int, [_CTX, _D, c_int, _P, _D, _D]),
+    "hessian_matvec": (c_int, [_CTX, _D, c_int, _D]),
     "get_stats": (c_int, [_CTX, POINTER(GliaStats)]),
     "reset_stats": (c_int, [_CTX]),
     "set_timing": (c_int, [_CTX, c_int]),

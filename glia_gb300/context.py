@@ -296,6 +296,14 @@ class Context:
             self._keep = []
         return J.value, dJ
 
+    def hessian_matvec(self, x):
+        """Gauss-Newton matvec y = H x of the p block (DerivativeOperatorsRD::evaluateHessian),
+        linearised at the last gradient evaluation or state solve."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros_like(x)
+        self._check(self.api.hessian_matvec(self._h, _dptr(x), x.size, _dptr(y)), "hessian_matvec")
+        return y
+
     def stats(self) -> dict:
         st = _abi.GliaStats()
         self._check(self.api.get_stats(self._h, ctypes.byref(st)), "get_stats")

@@ -219,18 +219,14 @@ int glia_set_c0(glia_ctx* ctx, const void* c0) {
   return guarded(ctx, [&](glia::EngineBase& e) { e.set_c0(c0); });
 }
 int glia_solve_state(glia_ctx* ctx, int linearized, const void* c0, void* c1) {
-  if (linearized != 0) {
-    if (ctx) ctx->err = "solveState: only linearized = 0 is supported in this version";
-    return GLIA_ERR_INVALID;
-  }
-  return guarded(ctx, [&](glia::EngineBase& e) { e.solve_state(c0, c1); });
+  return guarded(ctx, [&](glia::EngineBase& e) { e.solve_state(linearized, c0, c1); });
 }
 int glia_solve_adjoint(glia_ctx* ctx, int linearized, const void* pt, void* a0) {
-  if (linearized != 1) {
-    if (ctx) ctx->err = "solveAdjoint: only linearized = 1 is supported in this version";
-    return GLIA_ERR_INVALID;
-  }
-  return guarded(ctx, [&](glia::EngineBase& e) { e.solve_adjoint(pt, a0); });
+  return guarded(ctx, [&](glia::EngineBase& e) { e.solve_adjoint(linearized, pt, a0); });
+}
+int glia_hessian_matvec(glia_ctx* ctx, const double* x, int nx, double* y) {
+  if (!x || !y) return GLIA_ERR_INVALID;
+  return guarded(ctx, [&](glia::EngineBase& e) { e.hessian_matvec(x, nx, y); });
 }
 int glia_get_state(glia_ctx* ctx, int i, void* out) {
   if (!out) return GLIA_ERR_INVALID;

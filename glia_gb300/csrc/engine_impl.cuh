@@ -1109,10 +1109,61 @@ class Engine final : public EngineBase {
     adjoint_done_ = false;
     trick_at_state_ = trick;
   }
-  void solve_state(const void* c0, void* c1) override {
+  void solve_state(int linearized, const void* c0, void* c1) override {
+    if (linearized != 0 && linearized != 1)
+      throw Error(GLIA_ERR_INVALID, "solveState: linearized must be 0 or 1");
     if (c0) import_field(c0, c0_);
-    solve_state_internal();
+    if (linearized)
+      solve_state_linearized_internal();
+    else
+      solve_state_internal();
     if (c1) export_field(ct_, c1);
+  }
+
+  // PdeOperatorsRD::solveState(1) (src/pde/PdeOperators.cpp:235-316): the incremental forward
+  // from c~0 (in c0_), the logistic step linearised at the state c_i at the start of step i
+  // (reaction(1, i), :140-190: c~ *= e / (c_i e + 1 - c_i)^2). The state history of the last
+  // solveState(0) is read, never written; checkpointed runs recompute each segment's states
+  // from its checkpoint on the way.
+  void solve_state_linearized_internal() {
+    if (!state_done_)
+      throw Error(GLIA_ERR_STATE, "solveState(1) needs a preceding solveState(0) for its history");
+    st_.nb_state_solves++;
+    st_.diff_ksp_itr_state = 0;
+    vcopy(ct_, c0_);
+    auto lin_step = [&](const R* ci) {
+      if (order_ == 2) {
+        solve(ct_, dt_ / 2.0, nullptr, nullptr, 0.0, 0);
+        reaction_linearized(ct_, ci);
+        solve(ct_, dt_ / 2.0, nullptr, nullptr, 0.0, 0);
+      } else {
+        solve(ct_, dt_, nullptr, nullptr, 0.0, 0);
+        reaction_linearized(ct_, ci);
+      }
+    };
+    if (full()) {
+      for (int i = 0; i < nt_; i++) lin_step(c_hist_[i]);
+    } else {
+      const int S = (int)ckpt_.size();
+      for (int s = 0; s < S; s++) {
+        const int i0 = s * every_, i1 = std::min(nt_, (s + 1) * every_);
+        if (!(S == 1 && last_seg_resident_)) {
+          vcopy(seg_c_[0], ckpt_[s]);
+          vcopy(tmp2(), ckpt_[s]);
+          for (int i = i0; i + 1 < i1; i++) {  // recompute solves: which = 2
+            step(tmp2(), nullptr, seg_half_[i - i0], 2);
+            vcopy(seg_c_[i - i0 + 1], tmp2());
+          }
+          last_seg_resident_ = false;
+        }
+        for (int i = i0; i < i1; i++) lin_step(seg_c_[i - i0]);
+      }
+    }
+    sync_sweep();
+  }
+  void reaction_linearized(R* x, const R* c) {
+    GLIA_TIMED(KS_REACTION_LIN, FB() * 4,
+               k_reaction_lin<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, x, rho_, c, (R)dt_));
   }
 
   // adjoint step from alpha_{i+1} (in p0_) to alpha_i (PdeOperatorsRD::solveAdjoint body,
@@ -1172,7 +1223,9 @@ class Engine final : public EngineBase {
   }
 
   // PdeOperatorsRD::solveAdjoint(1) with the gradient time accumulation fused into the sweep.
-  void solve_adjoint_internal(bool accumulate) {
+  // linearized = 2 (incremental adjoint of the Hessian matvec) is the same sweep; like the
+  // reference it leaves p_[nt] of the full history untouched.
+  void solve_adjoint_internal(bool accumulate, int linearized = 1) {
     if (!state_done_) throw Error(GLIA_ERR_STATE, "solveAdjoint needs a preceding solveState");
     st_.nb_adjoint_solves++;
     st_.diff_ksp_itr_adj = 0;
@@ -1185,7 +1238,7 @@ class Engine final : public EngineBase {
       GLIA_LAUNCH_CHECK();
     }
     if (full()) {
-      vcopy(p_hist_[nt_], p0_);
+      if (linearized == 1) vcopy(p_hist_[nt_], p0_);
       if (accumulate && !ref_) grad_point(nt_, c_hist_[nt_], explicit_kappa);
       for (int i = nt_ - 1; i >= 0; i--) {
         const R* chalf = c_half_.empty() ? nullptr : c_half_[i];
@@ -1247,10 +1300,49 @@ class Engine final : public EngineBase {
     d_front<false>(spec_a, nullptr);
     d_back<EPI_SETUP>(spec_a, chat0, rhat_, what_, R(0));
   }
-  void solve_adjoint(const void* pt, void* a0) override {
+  void solve_adjoint(int linearized, const void* pt, void* a0) override {
+    if (linearized != 1 && linearized != 2)
+      throw Error(GLIA_ERR_INVALID, "solveAdjoint: linearized must be 1 or 2");
     if (pt) import_field(pt, pt_);
-    solve_adjoint_internal(false);
+    solve_adjoint_internal(false, linearized);
     if (a0) export_field(p0_, a0);
+  }
+
+  // DerivativeOperatorsRD::evaluateHessian (src/grad/DerivativeOperatorsRD.cpp:229-438), the
+  // Gauss-Newton matvec of the p block (no diffusivity inversion, :398-425): c~0 = Phi p~,
+  // incremental forward, p~_t = -O^T O c~(1), incremental adjoint, y = h^3 (beta Phi^T c~0 -
+  // Phi^T a~0), or y = beta p~ - h^3 Phi^T a~0 with the L2b regulariser. The state history of the
+  // last gradient evaluation (or solveState) is the linearisation point. Entries of y past np
+  // (kappa, rho) carry beta x for L2b and 0 otherwise.
+  void hessian_matvec(const double* x, int nxin, double* y) override {
+    if (nxin != nx())
+      throw Error(GLIA_ERR_INVALID, "x has " + std::to_string(nxin) + " entries, expected " +
+                                        std::to_string(nx()) + " (np + nk + nr)");
+    if (opt_.diffusivity_inversion)
+      throw Error(GLIA_ERR_INVALID,
+                  "evaluateHessian: only the p block (no diffusivity inversion) is supported");
+    if (!state_done_)
+      throw Error(GLIA_ERR_STATE, "evaluateHessian needs a preceding state solve or gradient");
+    const int np = opt_.np;
+    const double h = 2.0 * M_PI / g_.n, h3 = h * h * h;
+    phi_apply_into(c0_, x);
+    solve_state_linearized_internal();
+    R* zero = d1_buf();
+    GLIA_CUDA(cudaMemsetAsync(zero, 0, sizeof(R) * N_, stream_));
+    GLIA_TIMED(KS_OBS, FB() * 4,
+               k_obs_residual<R><<<red_blocks_, kThreads, 0, stream_>>>(N_, ct_, obs_, zero, pt_,
+                                                                        sc_, ws_));
+    solve_adjoint_internal(false, 2);
+    std::vector<double> pa(std::max(np, 1));
+    phi_applyT_from(p0_, pa.data());
+    const bool l2b = opt_.regularization_norm != 0;
+    if (l2b) {
+      for (int i = 0; i < nx(); i++) y[i] = opt_.beta * x[i] - (i < np ? h3 * pa[i] : 0.0);
+    } else {
+      phi_applyT_from(c0_, y);
+      for (int i = 0; i < np; i++) y[i] = opt_.beta * h3 * y[i] - h3 * pa[i];
+      for (int i = np; i < nx(); i++) y[i] = 0.0;
+    }
   }
   void get_state(int i, void* out) override {
     if (!state_done_ || !full() || i < 0 || i > nt_)

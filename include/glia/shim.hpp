@@ -260,6 +260,13 @@ class DerivativeOperatorsRD {
               : glia_eval_objective_and_gradient(ctx(), x.data(), (int)x.size(),
                                                  data->dt1().data(), J, dJ.data());
   }
+  // DerivativeOperatorsRD::evaluateHessian(Vec y, Vec x) (src/grad/DerivativeOperatorsRD.cpp:
+  // 229-438), the Gauss-Newton p block, linearised at the last evaluation
+  PetscErrorCode evaluateHessian(Vec& y, const Vec& x) {
+    int rc = sync_settings();
+    y.assign(x.size(), 0.0);
+    return rc ? rc : glia_hessian_matvec(ctx(), x.data(), (int)x.size(), y.data());
+  }
   glia_ctx* ctx() const { return pde_operators_->spec_ops_->ctx_; }
   bool all_gradients_ = false;  // extension: p, kappa and rho gradients in one sweep
   std::shared_ptr<PdeOperatorsRD> pde_operators_;

@@ -172,10 +172,13 @@ int glia_set_obs_filter(glia_ctx* ctx, const void* filter);
 /* Tumor::c_0_ (used by the derivative operators when flag_reaction_inv is set). */
 int glia_set_c0(glia_ctx* ctx, const void* c0);
 /* PdeOperatorsRD::solveState(int linearized) (src/pde/PdeOperators.cpp:235-316).
- * c0 may be NULL (use Tumor::c_0_); c1 may be NULL. linearized: 0 only in this version. */
+ * c0 may be NULL (use Tumor::c_0_); c1 may be NULL. linearized = 0: the state equation (fills
+ * the history); 1: the incremental forward around the history of the last linearized = 0 solve,
+ * the logistic step linearised at the state at each step's start (reaction(1, i), :140-190). */
 int glia_solve_state(glia_ctx* ctx, int linearized, const void* c0, void* c1);
 /* PdeOperatorsRD::solveAdjoint(int linearized) (src/pde/PdeOperators.cpp:372-420).
- * Needs a preceding glia_solve_state. a0 may be NULL. */
+ * Needs a preceding glia_solve_state. a0 may be NULL. linearized = 1: adjoint; 2: incremental
+ * adjoint of the Hessian matvec (same sweep, p_[nt] of the history left as it was). */
 int glia_solve_adjoint(glia_ctx* ctx, int linearized, const void* pt, void* a0);
 /* PdeOperatorsRD::c_[i] (FULL history only) / p_[i] (after an adjoint, FULL history only). */
 int glia_get_state(glia_ctx* ctx, int i, void* out);
@@ -191,6 +194,15 @@ int glia_eval_gradient(glia_ctx* ctx, const double* x, int nx, const void* d1, d
  * (src/grad/DerivativeOperatorsRD.cpp:130-226). */
 int glia_eval_objective_and_gradient(glia_ctx* ctx, const double* x, int nx, const void* d1,
                                      double* J, double* dJ);
+/* DerivativeOperatorsRD::evaluateHessian (src/grad/DerivativeOperatorsRD.cpp:229-438): the
+ * Gauss-Newton matvec y = H x of the p block (the branch without diffusivity inversion,
+ * :398-425): c~0 = Phi x, incremental forward (glia_solve_state 1), p~_t = -O^T O c~(1),
+ * incremental adjoint (glia_solve_adjoint 2), y = h^3 (beta Phi^T c~0 - Phi^T a~0), or
+ * beta x - h^3 Phi^T a~0 with the L2b regulariser. Linearised at the state history of the last
+ * gradient evaluation or state solve (so call it after glia_eval_* at the current iterate).
+ * x and y have nx = np + nk + nr entries (host doubles); entries past np are beta x (L2b) or 0.
+ * GLIA_ERR_INVALID when diffusivity_inversion is set (the kappa blocks are not provided). */
+int glia_hessian_matvec(glia_ctx* ctx, const double* x, int nx, double* y);
 
 int glia_get_stats(const glia_ctx* ctx, glia_stats* st);
 int glia_reset_stats(glia_ctx* ctx);

@@ -726,31 +726,39 @@ struct Ctx {
   }
 
   // ---- PdeOperatorsRD (src/pde/PdeOperators.cpp) ----
+  // linearized = 0 fills the history; linearized = 1 is the incremental forward around it, the
+  // reaction linearised at c_[i] (reaction(1, i) reads c_[iter], :153-156), history untouched.
   int solveState(int linearized) {
+    if (linearized != 0 && (!state_done || (int)c_hist.size() != nt + 1)) {
+      err = "solveState(1) needs a preceding solveState(0)";
+      return GLIA_ERR_STATE;
+    }
     st.nb_state_solves++;
     vcopy(ct.data(), c0.data(), N);
-    c_hist.assign(nt + 1, Field());
-    c_half.assign(adjoint_store ? nt : 0, Field());
-    c_hist[0] = ct;
+    if (linearized == 0) {
+      c_hist.assign(nt + 1, Field());
+      c_half.assign(adjoint_store ? nt : 0, Field());
+      c_hist[0] = ct;
+    }
     st.diff_ksp_itr_state = 0;
     for (int i = 0; i < nt; i++) {
       int rc;
       if (order == 2) {
         if ((rc = solve(ct.data(), dt / 2.0))) return rc;
         st.diff_ksp_itr_state += ksp_itr;
-        if (adjoint_store) c_half[i] = ct;
+        if (linearized == 0 && adjoint_store) c_half[i] = ct;
         reaction(ct.data(), c_hist[i].data(), linearized);
         if ((rc = solve(ct.data(), dt / 2.0))) return rc;
         st.diff_ksp_itr_state += ksp_itr;
       } else {
         if ((rc = solve(ct.data(), dt))) return rc;
         st.diff_ksp_itr_state += ksp_itr;
-        if (adjoint_store) c_half[i] = ct;
+        if (linearized == 0 && adjoint_store) c_half[i] = ct;
         reaction(ct.data(), c_hist[i].data(), linearized);
       }
-      c_hist[i + 1] = ct;
+      if (linearized == 0) c_hist[i + 1] = ct;
     }
-    state_done = true;
+    if (linearized == 0) state_done = true;
     return 0;
   }
   // reactionAdjoint (:318-370)
@@ -791,6 +799,32 @@ struct Ctx {
         if ((rc = reactionAdjoint(nt - i - 1))) return rc;
       }
       p_hist[nt - i - 1] = p0;
+    }
+    return 0;
+  }
+
+  // evaluateHessian (src/grad/DerivativeOperatorsRD.cpp:229-438), branch without diffusivity
+  // inversion (:398-425): Gauss-Newton matvec of the p block around the current history.
+  int hessian(const double* x, double* y) {
+    if (opt.diffusivity_inversion) {
+      err = "evaluateHessian: only the p block (no diffusivity inversion) is supported";
+      return GLIA_ERR_INVALID;
+    }
+    const int np_ = opt.np;
+    phi_apply(c0.data(), x);
+    int rc = solveState(1);
+    if (rc) return rc;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; i++) pt[i] = -(obs_filter[i] * (obs_filter[i] * ct[i]));
+    if ((rc = solveAdjoint(2))) return rc;
+    std::vector<double> pa(std::max(np_, 1));
+    phi_applyT(pa.data(), p0.data());
+    if (opt.regularization_norm != 0) {
+      for (int i = 0; i < nx(); i++) y[i] = opt.beta * x[i] - (i < np_ ? h3 * pa[i] : 0.0);
+    } else {
+      phi_applyT(y, c0.data());
+      for (int i = 0; i < np_; i++) y[i] = opt.beta * h3 * y[i] - h3 * pa[i];
+      for (int i = np_; i < nx(); i++) y[i] = 0.0;
     }
     return 0;
   }
@@ -1065,7 +1099,7 @@ int oracle_glia_set_c0(glia_ctx* ctx, const double* c0) {
   return GLIA_OK;
 }
 int oracle_glia_solve_state(glia_ctx* ctx, int linearized, const double* c0, double* c1) {
-  if (!ctx || linearized != 0) return GLIA_ERR_INVALID;
+  if (!ctx || (linearized != 0 && linearized != 1)) return GLIA_ERR_INVALID;
   if (c0) std::copy(c0, c0 + ctx->N, ctx->c0.begin());
   int rc = ctx->solveState(linearized);
   if (rc) return rc;
@@ -1073,12 +1107,20 @@ int oracle_glia_solve_state(glia_ctx* ctx, int linearized, const double* c0, dou
   return GLIA_OK;
 }
 int oracle_glia_solve_adjoint(glia_ctx* ctx, int linearized, const double* pt, double* a0) {
-  if (!ctx || linearized != 1) return GLIA_ERR_INVALID;
+  if (!ctx || (linearized != 1 && linearized != 2)) return GLIA_ERR_INVALID;
   if (pt) std::copy(pt, pt + ctx->N, ctx->pt.begin());
   int rc = ctx->solveAdjoint(linearized);
   if (rc) return rc;
   if (a0) std::copy(ctx->p0.begin(), ctx->p0.end(), a0);
   return GLIA_OK;
+}
+int oracle_glia_hessian_matvec(glia_ctx* ctx, const double* x, int nx, double* y) {
+  if (!ctx || !x || !y || nx != ctx->nx()) return GLIA_ERR_INVALID;
+  if (!ctx->state_done) {
+    ctx->err = "evaluateHessian needs a preceding state solve or gradient";
+    return GLIA_ERR_STATE;
+  }
+  return ctx->hessian(x, y);
 }
 int oracle_glia_get_state(glia_ctx* ctx, int i, double* out) {
   if (!ctx || !out || i < 0 || i >= (int)ctx->c_hist.size()) return GLIA_ERR_INVALID;
