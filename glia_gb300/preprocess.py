@@ -1,4 +1,5 @@
-"""Data preprocessing in front of the inversion: data-driven Gaussian centres.
+"""Data preprocessing in front of the inversion: data-driven Gaussian centres and the
+edema-based observation mask.
 
 `data_driven_centers` is Phi::setGaussians(Vec data) (src/mat/Phi.cpp:615-1004) for one process
 (the whole grid local, no neighbour exchange): on the lattice of points X with
@@ -84,3 +85,12 @@ def data_driven_centers(data: np.ndarray, sigma: float = 2 * np.pi / 256,
     else:
         comp = np.ones(len(sel), dtype=np.int64)
     return centers, comp, frac
+
+
+def edema_observation_mask(tc: np.ndarray, ed: np.ndarray, lam: float) -> np.ndarray:
+    """createEdemaBasedObservationMask (src/utils/Utils.cpp:567-590): O = 1 on the tumour core
+    (tc > 0.99), 0 on edema (ed > 0.99), lam elsewhere; the diagonal of the observation operator
+    for glia_set_obs_filter."""
+    tc = np.asarray(tc, dtype=np.float64)
+    ed = np.asarray(ed, dtype=np.float64)
+    return np.where(tc > 0.99, 1.0, np.where(ed > 0.99, 0.0, float(lam)))

@@ -6,7 +6,7 @@ import math
 import numpy as np
 import pytest
 
-from glia_gb300.preprocess import data_driven_centers, lattice_axis
+from glia_gb300.preprocess import data_driven_centers, edema_observation_mask, lattice_axis
 
 
 def _loops(data, sigma, thr, frac, spacing_factor=2.0):
@@ -79,3 +79,9 @@ def test_component_labels_and_lattice_rules():
     assert lattice_axis(16, 2.5)[:4] == [0, 2, 4, 6]
     with pytest.raises(ValueError):
         lattice_axis(16, 0.5)
+
+
+def test_edema_observation_mask():
+    tc = np.array([1.0, 0.0, 0.0, 1.0, 0.5])
+    ed = np.array([0.0, 1.0, 0.0, 1.0, 0.0])
+    assert np.array_equal(edema_observation_mask(tc, ed, 0.3), [1.0, 0.0, 0.3, 1.0, 0.3])
