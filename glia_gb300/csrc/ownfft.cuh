@@ -407,14 +407,16 @@ __global__ void __launch_bounds__(256, 2)
         u[a] = make_float2(E.x - O.y, E.y + O.x);
       }
     }
-    __syncthreads();  // the slot is this component's exchange area from here
+    // a line's 8 threads are lanes of one warp and touch only that line's region of the slot:
+    // the exchanges below need warp barriers only
+    __syncwarp();  // the line's region is this component's exchange area from here
     reg_dft<R1, +1>(u);
 #pragma unroll
     for (int k1 = 0; k1 < R1; k1++) {
       if (k1) u[k1] = cmul2(u[k1], twA[k1 * R2 + t]);
       S[k1 * R2 + (t ^ (k1 & (R2 - 1)))] = u[k1];
     }
-    __syncthreads();
+    __syncwarp();
     float2 z[KPT][R2];
 #pragma unroll
     for (int ii = 0; ii < KPT; ii++) {
@@ -430,21 +432,21 @@ __global__ void __launch_bounds__(256, 2)
       for (int k2 = 1; k2 < R2; k2++)
         if (k1) z[ii][k2] = cmul2(z[ii][k2], twB[k2 * R1 + k1]);
     }
-    __syncthreads();
+    __syncwarp();
 #pragma unroll
     for (int ii = 0; ii < KPT; ii++) {
       const int m1 = t + R2 * ii;
 #pragma unroll
       for (int k2 = 0; k2 < R2; k2++) S[k2 * R1 + (m1 ^ (k2 & (R1 - 1)))] = z[ii][k2];
     }
-    __syncthreads();
+    __syncwarp();
 #pragma unroll
     for (int m1 = 0; m1 < R1; m1++) u[m1] = S[t * R1 + (m1 ^ (t & (R1 - 1)))];
     reg_dft<R1, -1>(u);  // Z'[t + R2 k1'] = u[k1']
-    __syncthreads();
+    __syncwarp();
 #pragma unroll
     for (int k1 = 0; k1 < R1; k1++) S[t + R2 * k1] = u[k1];
-    __syncthreads();
+    __syncwarp();
     // R2C post-processing, packed, straight to global (in place)
     float2* out = Hc + (size_t)j * NP + (size_t)(blk * LB + l) * NQ;
 #pragma unroll
