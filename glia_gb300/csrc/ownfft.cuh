@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256, 2)
   float2* nyq = slG0 + NN * TS;  // kz = n/2 columns: [0, NN) of G_x, [NN, 2 NN) of G_0
   float2* sm = nyq + 2 * NN;
   float2* tw = sm + NN * T;
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw_g[i];
+  fill_twb<D, +1>(tw, tw_g);
   const int c = threadIdx.x % T, gi = threadIdx.x / T;
   const float2* Gx = reinterpret_cast<const float2*>(Gin);
   const float2* G0 = Gx + NS;
@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(256, 2)
   float2* zA = sm + NN * T;
   float2* zB = zA + NN;
   float2* tw = zB + NN;
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw_g[i];
+  fill_twb<D, -1>(tw, tw_g);
   const int c = threadIdx.x % T, gi = threadIdx.x / T;
   const float2* K = reinterpret_cast<const float2*>(Kin);
   float2* Mx = reinterpret_cast<float2*>(Mout);

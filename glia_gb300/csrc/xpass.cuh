@@ -191,12 +191,22 @@ __device__ __forceinline__ XCol xcol(const Geo& g, int q) {
   return c;
 }
 
+// Twiddles of the two-stage DFT in the order a thread reads them: twb[b R1 + k1] =
+// exp(S 2 pi i b k1 / N) for b < R2, k1 < R1 (16-byte aligned rows, read in pairs).
+template <class D, int S>
+__device__ __forceinline__ void fill_twb(float2* twb, const float2* tw256) {
+  for (int i = threadIdx.x; i < D::R1 * D::R2; i += blockDim.x) {
+    const int b = i / D::R1, k1 = i - b * D::R1;
+    twb[i] = tw_n<D::N, S>(tw256, b * k1);
+  }
+}
+
 // One n-point DFT along the tile's rows for this thread's column, sign S, decomposition D
 // (N = R1 R2 rows, T columns, 256 threads): in(m, b, a) is the input at row R2 a + b,
-// out(m2, k1, k2, y) receives X[k1 + R1 k2]. All threads of the CTA take part (two barriers);
-// mid() runs after the first, when every input has been read.
+// out(m2, k1, k2, y) receives X[k1 + R1 k2]; twb is the table of fill_twb<D, S>. All threads of
+// the CTA take part (two barriers); mid() runs after the first, when every input has been read.
 template <class D, int S, class In, class Mid, class Out>
-__device__ __forceinline__ void xdft(float2* sm, const float2* tw, int c, int gi, In&& in,
+__device__ __forceinline__ void xdft(float2* sm, const float2* twb, int c, int gi, In&& in,
                                      Mid&& mid, Out&& out) {
   constexpr int NN = D::N, R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
   constexpr int NB1 = R2 / GR, NB2 = R1 / GR;
@@ -207,10 +217,14 @@ __device__ __forceinline__ void xdft(float2* sm, const float2* tw, int c, int gi
 #pragma unroll
     for (int a = 0; a < R1; a++) u[a] = in(m, b, a);
     reg_dft<R1, S>(u);
+    const float4* w4 = reinterpret_cast<const float4*>(twb + b * R1);
 #pragma unroll
-    for (int k1 = 0; k1 < R1; k1++) {
-      if (k1) u[k1] = cmul2(u[k1], tw_n<NN, S>(tw, b * k1));
+    for (int k1 = 0; k1 < R1; k1 += 2) {
+      const float4 w = w4[k1 / 2];
+      if (k1) u[k1] = cmul2(u[k1], make_float2(w.x, w.y));
+      u[k1 + 1] = cmul2(u[k1 + 1], make_float2(w.z, w.w));
       sm[(k1 * R2 + b) * T + c] = u[k1];
+      sm[((k1 + 1) * R2 + b) * T + c] = u[k1 + 1];
     }
   }
   __syncthreads();
@@ -248,7 +262,7 @@ __global__ void __launch_bounds__(256, 2)
   float2* sm = slotP + (MODE == 1 ? NN * T : 0);
   float2* tw = sm + NN * T;
   if (MODE == 1 && sc->status != 0) return;
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw_g[i];
+  fill_twb<D, +1>(tw, tw_g);
   const int c = threadIdx.x % T, gi = threadIdx.x / T;
   const int plane = NN * g.nh, Ns = plane * NN;
   const int ntiles = plane / T;
@@ -377,8 +391,8 @@ __global__ void __launch_bounds__(256, 2)
   constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
   constexpr int NB2 = R1 / GR;
   __shared__ float2 sm[NN * T];
-  __shared__ float2 tw[256];
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw_g[i];
+  __shared__ __align__(16) float2 tw[256];
+  fill_twb<D, -1>(tw, tw_g);
   __syncthreads();
   if (EPI == EPI_CGW && sc->status != 0) return;
   const int c = threadIdx.x % T, gi = threadIdx.x / T;
@@ -457,7 +471,7 @@ __global__ void __launch_bounds__(256, 2)
   float2* sm = slots + 2 * NN * T;
   float2* tw = sm + NN * T;
   if (EPI == EPI_CGW && sc->status != 0) return;
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw_g[i];
+  fill_twb<D, -1>(tw, tw_g);
   const int c = threadIdx.x % T, gi = threadIdx.x / T;
   const int plane = NN * g.nh, Ns = plane * NN;
   const int ntiles = plane / T;
