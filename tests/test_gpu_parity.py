@@ -197,9 +197,15 @@ def test_fused_zpass_matches_cufft_3d_path(n, monkeypatch):
     assert rel_l2(out[0][1], out[1][1]) < 1e-5
 
 
+@pytest.mark.parametrize("path", ["own", "2d", "zpass"])
 @pytest.mark.parametrize("n", [64, 128])
-def test_fused_zpass_against_oracle(n, monkeypatch):
-    monkeypatch.setenv("GLIA_ZPASS", "1")
+def test_transform_paths_against_oracle(n, path, monkeypatch):
+    """D apply, state and gradient of the FP32 transform paths against the FP64 oracle: the
+    default own x / y / z kernels, the x pass around 2-D cuFFT, the fused z pass."""
+    if path == "zpass":
+        monkeypatch.setenv("GLIA_ZPASS", "1")
+    elif path == "2d":
+        monkeypatch.setenv("GLIA_XPASS", "2d")
     nt = 4
     wl, tissue, centers = small_problem(n, nt, n_gauss=8)
     o, g = orc(n), gpu(n, MIXED)
