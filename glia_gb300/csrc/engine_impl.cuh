@@ -462,6 +462,9 @@ class Engine final : public EngineBase {
       else if (which == 1)
         k_zpass<NN><<<std::min(own_res_[1], pw_blocks_), 256, zpass_smem_bytes<NN>(), stream_>>>(
             g3s_, kxx_, tw256_);
+      else if (tma_)
+        k_yfwd_tma<NN><<<std::min(own_res_[2], pw_blocks_), 256, yfwd_tma_smem_bytes<NN>(),
+                         stream_>>>(kmap_, g3r_, tw256_, sc_);
       else
         k_yfwd<NN><<<std::min(own_res_[2], pw_blocks_), 256, yfwd_smem_bytes<NN>(), stream_>>>(
             g3s_, g3r_, tw256_);
@@ -494,7 +497,14 @@ class Engine final : public EngineBase {
                                      per_sm(k_xfwd_own<NN, EPI_CGW>, fs)});
         own_res_[0] = sms_ * per_sm(k_yinv<NN>, yinv_smem_bytes<NN>());
         own_res_[1] = sms_ * per_sm(k_zpass<NN>, zpass_smem_bytes<NN>());
-        own_res_[2] = sms_ * per_sm(k_yfwd<NN>, yfwd_smem_bytes<NN>());
+        const char* te = std::getenv("GLIA_TMA");
+        tma_ = te && te[0] == '1';
+        own_res_[2] = sms_ * (tma_ ? per_sm(k_yfwd_tma<NN>, yfwd_tma_smem_bytes<NN>())
+                                   : per_sm(k_yfwd<NN>, yfwd_smem_bytes<NN>()));
+        // TMA view of the packed arrays K = [K_x, K_y, L_z]: 3 n^2 rows of n floats, tiles of
+        // 2T floats x n rows (used by k_yfwd<TMA = true>, GLIA_TMA=1)
+        if (tma_)
+          kmap_ = make_tmap_f32_2d(g3s_, (uint64_t)NN, 3ull * NN * NN, 2 * YDecomp<NN>::T, NN);
       } else {
         xres_inv_ = sms_ * std::min(per_sm(k_xinv<NN, 0, false>, xinv_smem_bytes<NN, 0>()),
                                     per_sm(k_xinv<NN, 1, false>, xinv_smem_bytes<NN, 1>()));
@@ -602,7 +612,21 @@ class Engine final : public EngineBase {
     ksp_itr_ = h.it;
     k_solve_stats_reset<<<1, 1, 0, stream_>>>(sc_);
     GLIA_LAUNCH_CHECK();
+    if (h.dev_fault) raise_device_fault();
     if (h.err_status < 0) finish_solve(SolveStatus{h.err_status, h.err_its, h.last_dp});
+  }
+  // a kernel's bounded wait ran out (its CTA stopped early): the results are invalid
+  [[noreturn]] void raise_device_fault() {
+    GLIA_CUDA(cudaMemsetAsync(&sc_->dev_fault, 0, sizeof(int), stream_));
+    GLIA_CUDA(cudaStreamSynchronize(stream_));
+    throw Error(GLIA_ERR_CUDA, "a device-side copy did not complete within its time limit");
+  }
+  void check_device_fault() {
+    if (ref_) return;
+    int f = 0;
+    GLIA_CUDA(cudaMemcpyAsync(&f, &sc_->dev_fault, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+    GLIA_CUDA(cudaStreamSynchronize(stream_));
+    if (f) raise_device_fault();
   }
 
   template <bool CGDIR>
@@ -790,6 +814,7 @@ class Engine final : public EngineBase {
   void apply_d(const void* c, void* dc) override {
     import_field(c, tmp_);
     applyD_into(p0_, tmp_);
+    check_device_fault();
     export_field(p0_, dc);
   }
   // spectrum of the normalised Weierstrass kernel for sigma, times h^3 / N
@@ -1813,6 +1838,8 @@ class Engine final : public EngineBase {
   float2* tw256_ = nullptr;
   int xres_inv_ = 0, xres_fwd_ = 0;  // resident CTAs of k_xinv / k_xfwd on this device
   int own_res_[3] = {0, 0, 0};       // ... of k_yinv, k_zpass, k_yfwd
+  CUtensorMap kmap_{};               // TMA map of the packed line arrays (k_yfwd)
+  bool tma_ = false;                 // k_yfwd stages with TMA copies (GLIA_TMA=1)
   bool own_ = false;  // own y and z passes (x pass on): no cuFFT inside the D apply
   float2* tw_ = nullptr;
   char* fft_ws_ = nullptr;

@@ -39,6 +39,8 @@ struct DevScalars {
   int err_its;
   int guard;             // WHILE-loop body executions of the current solve
   double last_dp;
+  int dev_fault;         // a bounded device wait ran out (1: TMA copy did not arrive)
+  int pad2;
 };
 
 __device__ __forceinline__ int conv_test(double rn, const DevScalars* s) {

@@ -29,6 +29,7 @@
 // Fo = (Z[k] - conj Z[n/2 - k]) / 2i.
 #pragma once
 
+#include "tma.cuh"
 #include "xpass.cuh"
 
 namespace glia {
@@ -274,6 +275,139 @@ __global__ void __launch_bounds__(256, 2)
     }
   }
   cp_async_wait<0>();
+}
+
+template <int NN>
+constexpr int yfwd_tma_smem_bytes() {  // 128 bytes of alignment slack, slots, exchange, tables, barriers
+  return 128 + (3 * NN * YDecomp<NN>::T + 2 * NN + 256) * (int)sizeof(float2) + 16;
+}
+
+// k_yfwd with its items loaded by the tensor-memory accelerator (GLIA_TMA=1): one tensor copy
+// per item from kmap (the three arrays as 3 n^2 rows of n floats, a tile = the box of 2T floats x
+// n rows), issued by one thread and completing on the slot's mbarrier. Same results as k_yfwd;
+// measured 4.57 TB/s against k_yfwd's 4.86 at 256^3, so k_yfwd (cp.async) is the default.
+template <int NN>
+__global__ void __launch_bounds__(256, 2)
+    k_yfwd_tma(const __grid_constant__ CUtensorMap kmap, float* __restrict__ Mout,
+               const float2* __restrict__ tw_g, DevScalars* __restrict__ sc) {
+  using D = YDecomp<NN>;
+  constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T, NB2 = R1 / GR;
+  constexpr int NQ = NN / 2, NH = NN / 2 + 1, CB = NQ / T;
+  constexpr int PS = NN * NH, NS = NN * PS;
+  constexpr int ntiles = NN * CB;
+  constexpr unsigned TILE_BYTES = NN * T * sizeof(float2);
+  extern __shared__ float4 yfwd_dyn[];
+  float2* slots = reinterpret_cast<float2*>(
+      (reinterpret_cast<uintptr_t>(yfwd_dyn) + 127) & ~static_cast<uintptr_t>(127));
+  float2* sm = slots + 2 * NN * T;
+  float2* zA = sm + NN * T;
+  float2* zB = zA + NN;
+  float2* tw = zB + NN;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tw + 256);
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_mbar_init();
+  }
+  fill_twb<D, -1>(tw, tw_g);
+  __syncthreads();
+  const int c = threadIdx.x % T, gi = threadIdx.x / T;
+  float2* Mx = reinterpret_cast<float2*>(Mout);
+  float2* Mr = Mx + NS;
+  const int mytiles =
+      (int)blockIdx.x < ntiles ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
+                               : 0;
+  const int nitems = 3 * mytiles;
+  auto slot = [&](int i) { return slots + (i & 1) * NN * T; };
+  auto issue = [&](int i) {  // after a CTA barrier that ends every read of the slot
+    if (threadIdx.x == 0 && i < nitems) {
+      const int t = (int)blockIdx.x + (i / 3) * (int)gridDim.x, j = i % 3;
+      const int x = t / CB, cb = t - x * CB;
+      fence_proxy_async();
+      mbar_arrive_expect_tx(&bars[i & 1], TILE_BYTES);
+      tma_load_2d(slot(i), &kmap, cb * 2 * T, j * NN * NN + x * NN, &bars[i & 1]);
+    }
+  };
+  // item i has landed (all threads; uniform result). On a timeout: record the fault, wait
+  // (bounded) for this CTA's copies still in flight (items i, i + 1) and report false.
+  // The thread that observed the completed phase orders the copy before the CTA barrier.
+  auto ready = [&](int i) {  // one thread waits on the barrier, the CTA barrier publishes it
+    const bool ok = threadIdx.x != 0 || mbar_wait(&bars[i & 1], (unsigned)((i >> 1) & 1));
+    if (!__syncthreads_or(!ok)) return true;
+    if (threadIdx.x == 0) {
+      atomicExch(&sc->dev_fault, 1);
+      for (int q = i; q < i + 2 && q < nitems; q++)
+        mbar_wait(&bars[q & 1], (unsigned)((q >> 1) & 1));
+    }
+    __syncthreads();
+    return false;
+  };
+  issue(0);
+  issue(1);
+  for (int it = 0; it < mytiles; it++) {
+    const int tile = (int)blockIdx.x + it * (int)gridDim.x;
+    const int x = tile / CB, cb = tile - x * CB, kz = cb * T + c;
+    const bool pk = kz == 0;
+    const int i0 = 3 * it;
+    if (!ready(i0)) return;
+    {
+      const float2* S = slot(i0);
+      xdft<D, -1>(
+          sm, tw, c, gi, [&](int, int b, int a) { return S[(R2 * a + b) * T + c]; },
+          [&] { issue(i0 + 2); },
+          [&](int, int k1, int k2, float2 y) {
+            const int ky = k1 + R1 * k2;
+            if (pk)
+              zA[ky] = y;
+            else
+              Mx[x * PS + ky * NH + kz] = y;
+          });
+    }
+    float2 dsum[NB2][R2];
+    if (!ready(i0 + 1)) return;
+    {
+      const float2* S = slot(i0 + 1);
+      xdft<D, -1>(
+          sm, tw, c, gi, [&](int, int b, int a) { return S[(R2 * a + b) * T + c]; },
+          [&] { issue(i0 + 3); },
+          [&](int m2, int k1, int k2, float2 y) {
+            const float w = (float)wavenum(k1 + R1 * k2, NN);
+            dsum[m2][k2] = make_float2(-w * y.y, w * y.x);
+          });
+    }
+    if (!ready(i0 + 2)) return;
+    {
+      const float2* S = slot(i0 + 2);
+      xdft<D, -1>(
+          sm, tw, c, gi, [&](int, int b, int a) { return S[(R2 * a + b) * T + c]; },
+          [&] { issue(i0 + 4); },
+          [&](int m2, int k1, int k2, float2 y) {
+            const int ky = k1 + R1 * k2;
+            const float2 d = make_float2(dsum[m2][k2].x + y.x, dsum[m2][k2].y + y.y);
+            if (pk)
+              zB[ky] = d;
+            else
+              Mr[x * PS + ky * NH + kz] = d;
+          });
+    }
+    if (cb == 0) {  // unpack the kz' = 0 column into kz = 0 and kz = n/2
+      if (c == 0) {
+        for (int ky = gi; ky < NN; ky += GR) {
+          const int km = (NN - ky) & (NN - 1);
+#pragma unroll
+          for (int h = 0; h < 2; h++) {
+            const float2 z = h ? zB[ky] : zA[ky];
+            const float2 zm = h ? zB[km] : zA[km];
+            const float2 s2 = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
+            const float2 d2 = make_float2(0.5f * (z.y + zm.y), -0.5f * (z.x - zm.x));
+            float2* M = h ? Mr : Mx;
+            M[x * PS + ky * NH] = s2;
+            M[x * PS + ky * NH + NQ] = d2;
+          }
+        }
+      }
+    }
+  }
 }
 
 // z transforms: n/2 = R1 R2 complex points per line, R2 threads per line, 256 / R2 lines per

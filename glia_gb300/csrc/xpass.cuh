@@ -208,7 +208,7 @@ __device__ __forceinline__ void fill_twb(float2* twb, const float2* tw256) {
 template <class D, int S, class In, class Mid, class Out>
 __device__ __forceinline__ void xdft(float2* sm, const float2* twb, int c, int gi, In&& in,
                                      Mid&& mid, Out&& out) {
-  constexpr int NN = D::N, R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
+  constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
   constexpr int NB1 = R2 / GR, NB2 = R1 / GR;
 #pragma unroll
   for (int m = 0; m < NB1; m++) {

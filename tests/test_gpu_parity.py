@@ -197,13 +197,15 @@ def test_fused_zpass_matches_cufft_3d_path(n, monkeypatch):
     assert rel_l2(out[0][1], out[1][1]) < 1e-5
 
 
-@pytest.mark.parametrize("path", ["own", "2d", "zpass"])
+@pytest.mark.parametrize("path", ["own", "own_tma", "2d", "zpass"])
 @pytest.mark.parametrize("n", [64, 128])
 def test_transform_paths_against_oracle(n, path, monkeypatch):
     """D apply, state and gradient of the FP32 transform paths against the FP64 oracle: the
     default own x / y / z kernels, the x pass around 2-D cuFFT, the fused z pass."""
     if path == "zpass":
         monkeypatch.setenv("GLIA_ZPASS", "1")
+    elif path == "own_tma":  # y-forward pass staged by TMA tensor copies
+        monkeypatch.setenv("GLIA_TMA", "1")
     elif path == "2d":
         monkeypatch.setenv("GLIA_XPASS", "2d")
     nt = 4
@@ -242,7 +244,7 @@ def test_repeated_adjoint_after_one_state_solve_checkpointed():
     assert rel_l2(a, f.solve_adjoint(pt)) < 1e-12
 
 
-@pytest.mark.parametrize("path", ["own", "2d"])
+@pytest.mark.parametrize("path", ["own", "own_tma", "2d"])
 @pytest.mark.parametrize("n", [64, 128, 256])
 def test_transform_paths_match_cufft_3d(n, path, monkeypatch):
     """FP32 D apply, state solve and gradient through the library's own x / y / z transform
@@ -254,6 +256,8 @@ def test_transform_paths_match_cufft_3d(n, path, monkeypatch):
     f = reference_test_field(n) + 0.1 * tissue.wm.reshape(-1)
     x = np.concatenate([np.linspace(0.1, 0.9, len(centers)), [wl.kappa, wl.rho]])
     out = []
+    if path == "own_tma":  # y-forward pass staged by TMA tensor copies
+        monkeypatch.setenv("GLIA_TMA", "1")
     for on in (path, "0"):
         monkeypatch.setenv("GLIA_XPASS", on)
         g = gpu(n, MIXED)
