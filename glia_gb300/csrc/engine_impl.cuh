@@ -358,11 +358,12 @@ class Engine final : public EngineBase {
     GLIA_LAUNCH_CHECK();
   }
 
-  // First half of a spectral D apply: the three spectra of k grad u in g3s_, from the spectrum
-  // src (plain) or from the new PCG direction p = P r + b p (CGDIR: src = r, pdir = p). With the
-  // x pass (FP32, n = 64 ... 256) the layout of g3s_ is (x, ky, kz) per component (the x
-  // transform is done by k_xinv / k_xfwd, cuFFT does batched 2-D (y, z) transforms); otherwise
-  // it is the full 3-D spectrum.
+  // First half of a spectral D apply, from the spectrum src (plain) or from the new PCG direction
+  // p = P r + b p (CGDIR: src = r, pdir = p), up to the spectra of k grad u that d_back
+  // diverges. Own transforms (default, FP32, n = 64 ... 256): k_xinv -> G in g3r_, k_yinv ->
+  // packed lines in g3s_, k_zpass (k multiplied there, in place), k_yfwd -> M in g3r_. "2d": the
+  // x pass writes (x, ky, kz) per component to g3s_ and cuFFT does batched 2-D (y, z)
+  // transforms around k_mul_k3. Otherwise g3s_ holds the full 3-D spectra.
   template <bool CGDIR>
   void d_front(const R* src, R* pdir) {
     if (own_) {  // no cuFFT: x, y, z passes of our own, k multiplied inside the z pass
