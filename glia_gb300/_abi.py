@@ -122,6 +122,7 @@ SIGNATURES = {
     "eval_gradient": (c_int, [_CTX, _D, c_int, _P, _D]),
     "eval_objective_and_gradient": (c_int, [_CTX, _D, c_int, _P, _D, _D]),
     "hessian_matvec": (c_int, [_CTX, _D, c_int, _D]),
+    "selftest_bounded_wait": (c_int, [_CTX]),
     "get_stats": (c_int, [_CTX, POINTER(GliaStats)]),
     "reset_stats": (c_int, [_CTX]),
     "set_timing": (c_int, [_CTX, c_int]),

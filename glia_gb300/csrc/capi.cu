@@ -224,6 +224,9 @@ int glia_solve_state(glia_ctx* ctx, int linearized, const void* c0, void* c1) {
 int glia_solve_adjoint(glia_ctx* ctx, int linearized, const void* pt, void* a0) {
   return guarded(ctx, [&](glia::EngineBase& e) { e.solve_adjoint(linearized, pt, a0); });
 }
+int glia_selftest_bounded_wait(glia_ctx* ctx) {
+  return guarded(ctx, [&](glia::EngineBase& e) { e.selftest_bounded_wait(); });
+}
 int glia_hessian_matvec(glia_ctx* ctx, const double* x, int nx, double* y) {
   if (!x || !y) return GLIA_ERR_INVALID;
   return guarded(ctx, [&](glia::EngineBase& e) { e.hessian_matvec(x, nx, y); });

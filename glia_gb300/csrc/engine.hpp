@@ -42,6 +42,7 @@ class EngineBase {
   virtual void get_adjoint(int i, void* out) = 0;
   virtual void evaluate(const double* x, int nx, const void* d1, double* J, double* dJ) = 0;
   virtual glia_stats stats() const = 0;
+  virtual void selftest_bounded_wait() = 0;
   virtual void reset_stats() = 0;
   virtual void set_timing(bool on) = 0;
   virtual int timing(int slot, const char** name, int64_t* launches, double* ms,

@@ -616,6 +616,25 @@ class Engine final : public EngineBase {
     if (h.dev_fault) raise_device_fault();
     if (h.err_status < 0) finish_solve(SolveStatus{h.err_status, h.err_its, h.last_dp});
   }
+  void selftest_bounded_wait() override {
+    if constexpr (!std::is_same<R, float>::value) {
+      throw Error(GLIA_ERR_INVALID, "selftest_bounded_wait: FP32 contexts only");
+    } else {
+      GLIA_CUDA(cudaStreamSynchronize(stream_));
+      k_selftest_wait<<<1, 32, 0, stream_>>>(&sc_->dev_fault);
+      GLIA_LAUNCH_CHECK();
+      int f = 0;
+      GLIA_CUDA(cudaMemcpyAsync(&f, &sc_->dev_fault, sizeof(int), cudaMemcpyDeviceToHost,
+                                stream_));
+      GLIA_CUDA(cudaStreamSynchronize(stream_));
+      GLIA_CUDA(cudaMemsetAsync(&sc_->dev_fault, 0, sizeof(int), stream_));
+      if (f != 1) throw Error(GLIA_ERR_CUDA, "bounded wait did not record its timeout");
+      // the context must still run kernels
+      k_solve_stats_reset<<<1, 1, 0, stream_>>>(sc_);
+      GLIA_LAUNCH_CHECK();
+      GLIA_CUDA(cudaStreamSynchronize(stream_));
+    }
+  }
   // a kernel's bounded wait ran out (its CTA stopped early): the results are invalid
   [[noreturn]] void raise_device_fault() {
     GLIA_CUDA(cudaMemsetAsync(&sc_->dev_fault, 0, sizeof(int), stream_));

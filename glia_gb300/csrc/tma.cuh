@@ -61,6 +61,19 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
+// One CTA waits on an mbarrier that nothing signals: the bounded wait must give up and record
+// the fault (glia_selftest_bounded_wait).
+static __global__ void k_selftest_wait(int* fault) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const bool ok = threadIdx.x != 0 || mbar_wait(&bar, 0);
+  if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicExch(fault, 1);
+}
+
 // Host: FP32 2-D tensor map over `rows` rows of `inner` floats (row pitch = inner floats), box
 // box_inner x box_rows, no swizzle, 256-byte L2 promotion, no out-of-range fill.
 inline CUtensorMap make_tmap_f32_2d(const void* base, uint64_t inner, uint64_t rows,

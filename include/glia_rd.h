@@ -232,6 +232,13 @@ int glia_get_timing(glia_ctx* ctx, int slot, const char** name, int64_t* launche
 int glia_mismatch_f32_noalloc(const float* c, const float* obs, const float* d, float* pt,
                               int64_t n, double* sumsq, void* stream);
 
+/* Diagnostic (extension; no counterpart in the reference): checks the bounded device waits the
+ * TMA staging relies on. One CTA waits on an mbarrier that no copy signals; the wait gives up
+ * after about 2^31 SM cycles (one second at 2 GHz) and records the fault in the context's device
+ * scalars, which this call reads and clears. Returns GLIA_OK when the fault was recorded and the
+ * context still runs kernels afterwards, GLIA_ERR_CUDA otherwise. FP32 contexts only. */
+int glia_selftest_bounded_wait(glia_ctx* ctx);
+
 #ifdef __cplusplus
 }
 #endif
