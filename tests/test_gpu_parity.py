@@ -269,3 +269,48 @@ def test_transform_paths_match_cufft_3d(n, path, monkeypatch):
     assert rel_l2(out[0][1], out[1][1]) < 1e-5
     assert abs(out[0][2][0] - out[1][2][0]) <= 1e-5 * abs(out[1][2][0])
     assert rel_l2(out[0][2][1], out[1][2][1]) < 1e-4
+
+
+@pytest.mark.parametrize("variant", ["lie", "nk3_nr3", "phi_store_l2b", "obs_threshold",
+                                     "reaction_inv", "sinusoidal"])
+def test_gradient_variants_on_own_transforms(variant):
+    """J and grad J of the mixed path at 64^3 (the library's own x / y / z transform kernels)
+    against the FP64 oracle, over the reference's model and optimiser options: Lie splitting,
+    three diffusivity / reaction classes (explicit kappa gradient), stored Phi with the L2b
+    regulariser, a thresholded observation operator, reaction inversion, sinusoidal tissue and
+    diffusivity."""
+    n, nt = 64, 3
+    wl, tissue, centers = small_problem(n, nt, n_gauss=8)
+    d1 = observation(wl, tissue, centers)
+    np_ = len(centers)
+    o, g = orc(n), gpu(n, MIXED)
+    nk = nr = 1
+    for ctx in (o, g):
+        configure(ctx, wl, tissue, centers)
+        ctx.set_obs_filter(np.ones(n ** 3))
+        if variant == "lie":
+            ctx.set_time(wl.dt, nt, 1)
+        elif variant == "nk3_nr3":
+            ctx.set_coefficients(k=wl.kappa, rho=wl.rho, k_gm_wm=0.2, k_glm_wm=0.1,
+                                 r_gm_wm=0.5, r_glm_wm=0.2)
+            ctx.set_opt(nk=3, nr=3)
+            nk = nr = 3
+        elif variant == "phi_store_l2b":
+            ctx.set_opt(phi_store=1, regularization_norm=1, beta=0.1)
+        elif variant == "obs_threshold":
+            ctx.set_obs_threshold(d1, 0.3)
+        elif variant == "reaction_inv":
+            ctx.set_opt(flag_reaction_inv=1, all_gradients=0)
+            ctx.set_c0(o.phi_apply(np.linspace(0.2, 1.0, np_)))
+        elif variant == "sinusoidal":
+            ctx.set_tissue_sinusoidal()
+            ctx.set_diffusivity_sinusoidal(1e-2)
+    if nk == 3:
+        x = np.concatenate([np.linspace(0.1, 0.9, np_), [wl.kappa, 0.2 * wl.kappa, 0.1 * wl.kappa],
+                            [wl.rho, 0.5 * wl.rho, 0.2 * wl.rho]])
+    else:
+        x = np.concatenate([np.linspace(0.1, 0.9, np_), [wl.kappa, wl.rho]])
+    Jo, gro = o.eval_objective_and_gradient(x, d1)
+    Jg, grg = g.eval_objective_and_gradient(x, d1)
+    assert abs(Jg - Jo) <= 1e-4 * abs(Jo)
+    assert rel_l2(grg, gro) < GRAD_TOL
