@@ -2,8 +2,8 @@
 // forward / adjoint / gradient path.
 //
 // This file restates, in plain C++17 + OpenMP and double precision, the algorithm of the
-// reference (ShashankSubramanian/GLIA). It is the checker for the CUDA library and the timed CPU
-// baseline; the product never links, loads or calls it. Only tests/, __graft_entry__.smoke() and
+// reference (ShashankSubramanian/GLIA). It is the reference the CUDA library is tested against and the timed
+// CPU baseline; the product never links, loads or calls it. Only tests/, __graft_entry__.smoke() and
 // bench.py's CPU legs use it.
 //
 // Pins (see tests/test_oracle_pins.py):

@@ -1,6 +1,6 @@
 """TEST INFRASTRUCTURE ONLY: Python handle on the FP64 CPU oracle (oracle/glia_oracle.cpp).
 
-Used by tests/, __graft_entry__.smoke() and bench.py's CPU baseline legs as the checker; the
+Used by tests/, __graft_entry__.smoke() and bench.py's CPU baseline legs to check results; the
 product path never imports this module. `load()` builds the oracle with its Makefile when the
 shared library is missing or older than its source.
 """

@@ -1,4 +1,4 @@
-"""CUDA library against the FP64 CPU oracle on the same seeded inputs (GPU machine only).
+"""CUDA library against the FP64 CPU oracle on the same seeded inputs (needs a GPU).
 
 Every comparison goes through the C-ABI (include/glia_rd.h). Bars: FP64 state rel-L2 <= 1e-5,
 mixed (FP32 bulk, FP64 reductions) <= 1e-4, gradients <= 1e-4; PCG iteration counts equal for
