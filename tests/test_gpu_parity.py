@@ -184,12 +184,13 @@ def test_graph_loop_equals_host_loop(prec):
 @pytest.mark.parametrize("n", [64, 128, 256])
 def test_fused_zpass_matches_cufft_3d_path(n, monkeypatch):
     """FP32 D apply with the fused z pass (k_zpass_mulk between 2-D cuFFT passes) against the
-    three-dimensional cuFFT transforms around k_mul_k3."""
+    three-dimensional cuFFT transforms around k_mul_k3 (GLIA_XPASS=0)."""
     wl, tissue, centers = small_problem(n, 2, n_gauss=8)
     f = reference_test_field(n) + 0.1 * tissue.wm.reshape(-1)
     out = []
-    for on in ("1", "0"):
-        monkeypatch.setenv("GLIA_ZPASS", on)
+    for zpass, xpass in (("1", "own"), ("0", "0")):
+        monkeypatch.setenv("GLIA_ZPASS", zpass)
+        monkeypatch.setenv("GLIA_XPASS", xpass)  # "0": batched 3-D cuFFT
         g = gpu(n, MIXED)
         configure(g, wl, tissue, centers)
         out.append((g.apply_d(f), g.solve_state(g.phi_apply(np.linspace(0.2, 1, 8)))))
@@ -225,6 +226,34 @@ def test_transform_paths_against_oracle(n, path, monkeypatch):
     _, gro = o.eval_objective_and_gradient(x, d1)
     _, grg = g.eval_objective_and_gradient(x, d1)
     assert rel_l2(grg, gro) < GRAD_TOL
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+def test_full_size_d_apply_and_cn_solve(prec):
+    """256^3, the size of the gradient-evaluation workload: D apply and one Crank-Nicolson
+    diffusion solve against the oracle, equal PCG iteration counts (FP64), and two properties of
+    the operator that hold at every size: D u sums to zero (the divergence has no mean) and D is
+    symmetric, <D u, v> = <u, D v>; the solve conserves mass."""
+    n = 256
+    wl, tissue, centers = small_problem(n, 2, n_gauss=1)
+    o, g = orc(n), gpu(n, prec)
+    for ctx in (o, g):
+        configure(ctx, wl, tissue, centers)
+    f = reference_test_field(n) + 0.1 * tissue.wm.reshape(-1)
+    v = reference_test_field(n)[::-1].copy() + tissue.gm.reshape(-1)
+    tol = 1e-11 if prec == FP64 else 2e-5
+    df = g.apply_d(f)
+    assert rel_l2(df, o.apply_d(f)) < tol
+    dv = g.apply_d(v)
+    assert abs(df.sum()) <= tol * np.abs(df).sum()
+    assert abs(np.dot(df, v) - np.dot(f, dv)) <= tol * np.linalg.norm(df) * np.linalg.norm(v)
+    cg, co = f.copy(), f.copy()
+    its_g = g.diffusion_solve(cg, wl.dt)
+    its_o = o.diffusion_solve(co, wl.dt)
+    assert rel_l2(cg, co) < STATE_TOL[prec]
+    if prec == FP64:
+        assert its_g == its_o
+    assert abs(cg.sum() - f.sum()) <= (1e-12 if prec == FP64 else 1e-5) * np.abs(f).sum()
 
 
 def test_repeated_adjoint_after_one_state_solve_checkpointed():
