@@ -114,6 +114,7 @@ SIGNATURES = {
     "set_obs_threshold": (c_int, [_CTX, _P, c_double]),
     "set_obs_filter": (c_int, [_CTX, _P]),
     "set_c0": (c_int, [_CTX, _P]),
+    "set_secondary_coefficients": (c_int, [_CTX, c_double, c_double, c_double]),
     "solve_state": (c_int, [_CTX, c_int, _P, _P]),
     "solve_adjoint": (c_int, [_CTX, c_int, _P, _P]),
     "get_state": (c_int, [_CTX, c_int, _P]),

@@ -226,6 +226,10 @@ class Context:
             self._keep = []
         return pout
 
+    def set_secondary_coefficients(self, k1, k2=0.0, k3=0.0):
+        """DiffCoef::setSecondaryCoefficients: the diffusivity direction of solve_state(2)."""
+        self._call("set_secondary_coefficients", self.api.set_secondary_coefficients, k1, k2, k3)
+
     def solve_state(self, c0=None, out=None, linearized=0):
         self._keep = []
         try:

@@ -218,6 +218,9 @@ int glia_set_c0(glia_ctx* ctx, const void* c0) {
   if (!c0) return GLIA_ERR_INVALID;
   return guarded(ctx, [&](glia::EngineBase& e) { e.set_c0(c0); });
 }
+int glia_set_secondary_coefficients(glia_ctx* ctx, double k1, double k2, double k3) {
+  return guarded(ctx, [&](glia::EngineBase& e) { e.set_secondary_coefficients(k1, k2, k3); });
+}
 int glia_solve_state(glia_ctx* ctx, int linearized, const void* c0, void* c1) {
   return guarded(ctx, [&](glia::EngineBase& e) { e.solve_state(linearized, c0, c1); });
 }

@@ -35,6 +35,7 @@ class EngineBase {
   virtual void set_obs_threshold(const void* data, double thr) = 0;
   virtual void set_obs_filter(const void* f) = 0;
   virtual void set_c0(const void* c0) = 0;
+  virtual void set_secondary_coefficients(double k1, double k2, double k3) = 0;
   virtual void solve_state(int linearized, const void* c0, void* c1) = 0;
   virtual void solve_adjoint(int linearized, const void* pt, void* a0) = 0;
   virtual void hessian_matvec(const double* x, int nx, double* y) = 0;

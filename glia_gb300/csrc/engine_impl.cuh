@@ -837,6 +837,39 @@ class Engine final : public EngineBase {
     check_device_fault();
     export_field(p0_, dc);
   }
+  // DiffCoef::setSecondaryCoefficients (src/mat/DiffCoef.cpp:44-58): the Hessian's diffusivity
+  // direction k~ = k1 wm + k2 gm + k3 csf (k2, k3 from the current ratios when nk = 1)
+  void set_secondary_coefficients(double k1, double k2, double k3) override {
+    if (opt_.nk == 1) {
+      k2 = k_gm_wm_ * k1;
+      k3 = k_glm_wm_ * k1;
+    }
+    if (!ksec_) ksec_ = fld();
+    k_assemble_secondary<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, ksec_, wm_, gm_, csf_, k1,
+                                                                   k2, k3);
+    GLIA_LAUNCH_CHECK();
+    ksec_set_ = true;
+  }
+  // DiffCoef::applyDWithSecondaryCoeffs (:273-300): out = div(k~ grad in), out may alias in. The
+  // fused paths read the k field through kxx_, which points at k~ for this one apply.
+  void applyD_secondary_into(R* out, const R* in) {
+    if (!ksec_set_) throw Error(GLIA_ERR_STATE, "no secondary diffusion coefficients set");
+    if (ref_) {
+      ref_gradient(t_[4], t_[5], t_[6], in);
+      vmult(t_[1], ksec_, t_[4]);
+      vmult(t_[2], ksec_, t_[5]);
+      vmult(t_[3], ksec_, t_[6]);
+      ref_divergence(out, t_[1], t_[2], t_[3]);
+      return;
+    }
+    struct Restore {
+      R*& k;
+      R* saved;
+      ~Restore() { k = saved; }
+    } restore{kxx_, kxx_};
+    kxx_ = ksec_;
+    applyD_into(out, in);
+  }
   // spectrum of the normalised Weierstrass kernel for sigma, times h^3 / N
   // (SpectralOperators::weierstrassSmoother, src/grad/SpectralOperators.cpp:264-381)
   const R* smoother_kernel(double sigma) {
@@ -1073,6 +1106,9 @@ class Engine final : public EngineBase {
         p_hist_.resize(nt_ + 1);
         for (auto& f : c_hist_) f = fld();
         for (auto& f : p_hist_) f = fld();
+        // p_[nt] is read by the Hessian's kappa rows before any adjoint may have set it; the
+        // reference's history vectors start at 0 (src/pde/PdeOperators.cpp:27-31)
+        GLIA_CUDA(cudaMemsetAsync(p_hist_[nt_], 0, N_ * sizeof(R), stream_));
         if (store_half) {
           c_half_.resize(nt_);
           for (auto& f : c_half_) f = fld();
@@ -1148,6 +1184,7 @@ class Engine final : public EngineBase {
       vcopy(seg_c_[nt_ - last0], ct_);
       if (trick) r2c(r2c1_, ct_, seg_chat_[nt_ - last0]);
       last_seg_resident_ = true;
+      vcopy(cfin(), ct_);  // c_[nt] for the Hessian's kappa rows
     }
     sync_sweep();
     state_done_ = true;
@@ -1155,11 +1192,11 @@ class Engine final : public EngineBase {
     trick_at_state_ = trick;
   }
   void solve_state(int linearized, const void* c0, void* c1) override {
-    if (linearized != 0 && linearized != 1)
-      throw Error(GLIA_ERR_INVALID, "solveState: linearized must be 0 or 1");
+    if (linearized < 0 || linearized > 2)
+      throw Error(GLIA_ERR_INVALID, "solveState: linearized must be 0, 1 or 2");
     if (c0) import_field(c0, c0_);
     if (linearized)
-      solve_state_linearized_internal();
+      solve_state_linearized_internal(linearized);
     else
       solve_state_internal();
     if (c1) export_field(ct_, c1);
@@ -1167,27 +1204,41 @@ class Engine final : public EngineBase {
 
   // PdeOperatorsRD::solveState(1) (src/pde/PdeOperators.cpp:235-316): the incremental forward
   // from c~0 (in c0_), the logistic step linearised at the state c_i at the start of step i
-  // (reaction(1, i), :140-190: c~ *= e / (c_i e + 1 - c_i)^2). The state history of the last
-  // solveState(0) is read, never written; checkpointed runs recompute each segment's states
+  // (reaction(1, i), :140-190: c~ *= e / (c_i e + 1 - c_i)^2). mode 2 (solveState(2)) adds the
+  // diffusivity direction's sources around each step (solveIncremental, :192-233): before the
+  // first diffusion half step c~ += dt/4 D~(0.5 (c_i + c_i+1) + c_i), after the second
+  // c~ += dt/4 D~(0.5 (c_i + c_i+1) + c_i+1), D~ the D apply with k~. The state history of the
+  // last solveState(0) is read, never written; checkpointed runs recompute each segment's states
   // from its checkpoint on the way.
-  void solve_state_linearized_internal() {
+  void solve_state_linearized_internal(int mode = 1) {
     if (!state_done_)
       throw Error(GLIA_ERR_STATE, "solveState(1) needs a preceding solveState(0) for its history");
+    if (mode == 2 && !ksec_set_)
+      throw Error(GLIA_ERR_STATE, "solveState(2) needs the secondary diffusion coefficients");
     st_.nb_state_solves++;
     st_.diff_ksp_itr_state = 0;
     vcopy(ct_, c0_);
-    auto lin_step = [&](const R* ci) {
+    auto source = [&](const R* ci, const R* cj, int m) {
+      if (!inc_) inc_ = fld();
+      k_incr_mix<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, inc_, ci, cj, m);
+      GLIA_LAUNCH_CHECK();
+      applyD_secondary_into(inc_, inc_);
+      vaxpy_any(ct_, (dt_ / 2.0) / 2.0, inc_);
+    };
+    auto lin_step = [&](const R* ci, const R* cj) {
+      if (mode == 2) source(ci, cj, 1);
       if (order_ == 2) {
         solve(ct_, dt_ / 2.0, nullptr, nullptr, 0.0, 0);
         reaction_linearized(ct_, ci);
         solve(ct_, dt_ / 2.0, nullptr, nullptr, 0.0, 0);
+        if (mode == 2) source(ci, cj, 2);
       } else {
         solve(ct_, dt_, nullptr, nullptr, 0.0, 0);
         reaction_linearized(ct_, ci);
       }
     };
     if (full()) {
-      for (int i = 0; i < nt_; i++) lin_step(c_hist_[i]);
+      for (int i = 0; i < nt_; i++) lin_step(c_hist_[i], c_hist_[i + 1]);
     } else {
       const int S = (int)ckpt_.size();
       for (int s = 0; s < S; s++) {
@@ -1195,13 +1246,16 @@ class Engine final : public EngineBase {
         if (!(S == 1 && last_seg_resident_)) {
           vcopy(seg_c_[0], ckpt_[s]);
           vcopy(tmp2(), ckpt_[s]);
-          for (int i = i0; i + 1 < i1; i++) {  // recompute solves: which = 2
+          // recompute solves (which = 2) up to the segment's last step start, or its end when
+          // the sources need c_i+1
+          const int iend = mode == 2 ? i1 : i1 - 1;
+          for (int i = i0; i < iend; i++) {
             step(tmp2(), nullptr, seg_half_[i - i0], 2);
             vcopy(seg_c_[i - i0 + 1], tmp2());
           }
           last_seg_resident_ = false;
         }
-        for (int i = i0; i < i1; i++) lin_step(seg_c_[i - i0]);
+        for (int i = i0; i < i1; i++) lin_step(seg_c_[i - i0], seg_c_[i - i0 + 1]);
       }
     }
     sync_sweep();
@@ -1270,11 +1324,13 @@ class Engine final : public EngineBase {
   // PdeOperatorsRD::solveAdjoint(1) with the gradient time accumulation fused into the sweep.
   // linearized = 2 (incremental adjoint of the Hessian matvec) is the same sweep; like the
   // reference it leaves p_[nt] of the full history untouched.
-  void solve_adjoint_internal(bool accumulate, int linearized = 1) {
+  // skip_final leaves out the t = 1 term of the accumulation (the Hessian adds its own).
+  void solve_adjoint_internal(bool accumulate, int linearized = 1, bool skip_final = false) {
     if (!state_done_) throw Error(GLIA_ERR_STATE, "solveAdjoint needs a preceding solveState");
     st_.nb_adjoint_solves++;
     st_.diff_ksp_itr_adj = 0;
     vcopy(p0_, pt_);
+    if (!full() && linearized == 1) vcopy(pnt(), p0_);  // the reference's p_[nt]
     const bool trick = trick_at_state_ && kappa_trick_ok();
     const bool explicit_kappa = accumulate && !trick;
     kappa_used_trick_ = trick;
@@ -1284,17 +1340,18 @@ class Engine final : public EngineBase {
     }
     if (full()) {
       if (linearized == 1) vcopy(p_hist_[nt_], p0_);
-      if (accumulate && !ref_) grad_point(nt_, c_hist_[nt_], explicit_kappa);
+      if (accumulate && !ref_ && !skip_final) grad_point(nt_, c_hist_[nt_], explicit_kappa);
       for (int i = nt_ - 1; i >= 0; i--) {
         const R* chalf = c_half_.empty() ? nullptr : c_half_[i];
+        const bool kdot = accumulate && trick && !(skip_final && i + 1 == nt_);
         if (order_ == 2) {
-          solve(p0_, dt_ / 2.0, nullptr, (accumulate && trick) ? chat_hist_[i + 1] : nullptr,
+          solve(p0_, dt_ / 2.0, nullptr, kdot ? chat_hist_[i + 1] : nullptr,
                 ((i + 1 == nt_) ? 0.5 : 1.0) * dt_, 1);
           if (!chalf) chalf = recompute_half(c_hist_[i]);
           reaction_adjoint(chalf);
           solve(p0_, dt_ / 2.0, nullptr, nullptr, 0.0, 1);
         } else {
-          solve(p0_, dt_, nullptr, (accumulate && trick) ? chat_hist_[i + 1] : nullptr,
+          solve(p0_, dt_, nullptr, kdot ? chat_hist_[i + 1] : nullptr,
                 ((i + 1 == nt_) ? 0.5 : 1.0) * dt_, 1);
           if (!chalf) chalf = recompute_half(c_hist_[i]);
           reaction_adjoint(chalf);
@@ -1306,7 +1363,7 @@ class Engine final : public EngineBase {
     } else {
       // checkpointed: recompute each segment forward from its checkpoint, then sweep it back
       const int S = (int)ckpt_.size();
-      if (accumulate) grad_point(nt_, ct_, explicit_kappa);
+      if (accumulate && !skip_final) grad_point(nt_, ct_, explicit_kappa);
       for (int s = S - 1; s >= 0; s--) {
         const int i0 = s * every_, i1 = std::min(nt_, (s + 1) * every_);
         // the last segment is still resident from the forward sweep (first adjoint only)
@@ -1322,7 +1379,7 @@ class Engine final : public EngineBase {
         }
         for (int i = i1 - 1; i >= i0; i--) {
           adjoint_step(i, seg_half_[i - i0], trick ? seg_chat_[i - i0 + 1] : nullptr,
-                       accumulate && trick);
+                       accumulate && trick && !(skip_final && i + 1 == nt_));
           if (accumulate) grad_point(i, seg_c_[i - i0], explicit_kappa);
         }
         if (s == 0 && accumulate && trick) kappa_dot_at(seg_chat_[0], 0.5 * dt_);
@@ -1335,6 +1392,19 @@ class Engine final : public EngineBase {
   R* tmp2() {
     if (!tmp2_) tmp2_ = fld();
     return tmp2_;
+  }
+  // checkpointed runs: the reference's p_[nt] (final condition of the last linearized = 1
+  // adjoint, 0 before the first) and c_[nt] (state at t = 1 of the last forward)
+  R* pnt() {
+    if (!pnt_) {
+      pnt_ = fld();
+      GLIA_CUDA(cudaMemsetAsync(pnt_, 0, N_ * sizeof(R), stream_));
+    }
+    return pnt_;
+  }
+  R* cfin() {
+    if (!cfin_) cfin_ = fld();
+    return cfin_;
   }
   // acc[6] += w <c_0, D alpha_0>: a D apply on alpha_0 whose spectral epilogue takes the dot
   void kappa_dot_at(const R* chat0, double w) {
@@ -1363,11 +1433,12 @@ class Engine final : public EngineBase {
     if (nxin != nx())
       throw Error(GLIA_ERR_INVALID, "x has " + std::to_string(nxin) + " entries, expected " +
                                         std::to_string(nx()) + " (np + nk + nr)");
-    if (opt_.diffusivity_inversion)
-      throw Error(GLIA_ERR_INVALID,
-                  "evaluateHessian: only the p block (no diffusivity inversion) is supported");
     if (!state_done_)
       throw Error(GLIA_ERR_STATE, "evaluateHessian needs a preceding state solve or gradient");
+    if (opt_.diffusivity_inversion) {
+      hessian_diffusivity(x, y);
+      return;
+    }
     const int np = opt_.np;
     const double h = 2.0 * M_PI / g_.n, h3 = h * h * h;
     phi_apply_into(c0_, x);
@@ -1388,6 +1459,78 @@ class Engine final : public EngineBase {
       for (int i = 0; i < np; i++) y[i] = opt_.beta * h3 * y[i] - h3 * pa[i];
       for (int i = np; i < nx(); i++) y[i] = 0.0;
     }
+  }
+  // evaluateHessian with diffusivity inversion (src/grad/DerivativeOperatorsRD.cpp:244-397):
+  // y = [Hpp p~ + Hpk k~; Hkp p~ + Hkk k~]. Two incremental forward / adjoint pairs around the
+  // state history of the last gradient evaluation: c~0 = Phi p~ with solveState(1), then
+  // c~0 = 0 with the diffusivity direction k~ (x's kappa entries) and solveState(2); each adjoint
+  // starts from -O^T O c~(1). p rows: h^3 (beta Phi^T Phi p~ - Phi^T a~0) - h^3 Phi^T a~0'.
+  // kappa rows: the gradDiffusion quadrature with a~ in place of the adjoint; its t = 1 term
+  // takes the reference's p_[nt], which solveAdjoint(2) leaves at the final condition of the last
+  // linearized = 1 adjoint. Rows past np + nk (rho) are 0 (the reference leaves them as the
+  // caller's y).
+  void hessian_diffusivity(const double* x, double* y) {
+    const int np = opt_.np, nk = opt_.nk;
+    const double h = 2.0 * M_PI / g_.n, h3 = h * h * h;
+    std::fill(y, y + nx(), 0.0);
+    const int npp = std::max({np, phi_np_, 1});
+    std::vector<double> pa(npp), pc(npp);
+    const bool trick = !ref_ && trick_at_state_ && kappa_trick_ok();
+    // incremental forward (mode 1 / 2), adjoint, Phi^T a~0 into pa, kappa rows into rows
+    auto pair = [&](int mode, double* rows) {
+      solve_state_linearized_internal(mode);
+      R* zero = d1_buf();
+      GLIA_CUDA(cudaMemsetAsync(zero, 0, sizeof(R) * N_, stream_));
+      GLIA_TIMED(KS_OBS, FB() * 4,
+                 k_obs_residual<R><<<red_blocks_, kThreads, 0, stream_>>>(N_, ct_, obs_, zero,
+                                                                          pt_, sc_, ws_));
+      double acc[8];
+      if (ref_) {
+        solve_adjoint_internal(false, 2);
+        phi_applyT_from(p0_, pa.data());
+        ref_time_integrals(acc);  // the stored p_[nt] is the reference's stale one
+      } else {
+        solve_adjoint_internal(true, 2, true);
+        phi_applyT_from(p0_, pa.data());
+        // the t = 1 term with p_[nt] and c_[nt]
+        vcopy(p0_, full() ? p_hist_[nt_] : pnt());
+        const R* cn = full() ? c_hist_[nt_] : cfin();
+        if (trick) {
+          const R* chat_n = chat_;
+          if (full())
+            chat_n = chat_hist_[nt_];
+          else
+            r2c(r2c1_, cn, chat_);
+          kappa_dot_at(chat_n, 0.5 * dt_);
+        } else {
+          grad_point(nt_, cn, true);
+        }
+        GLIA_CUDA(cudaMemcpyAsync(hsc_, sc_, sizeof(DevScalars), cudaMemcpyDeviceToHost, stream_));
+        GLIA_CUDA(cudaStreamSynchronize(stream_));
+        std::memcpy(acc, hsc_->acc, sizeof(acc));
+      }
+      rows[0] = rows[1] = rows[2] = 0.0;
+      if (trick) {
+        rows[0] = -acc[6] / k_scale_ * h3;  // <wm + r gm, grad c . grad a~> = -<c, D a~>/kappa
+      } else {
+        rows[0] = acc[0] * h3;
+        if (nk == 1) rows[0] += acc[1] * h3 * k_gm_wm_;
+        if (nk > 1) rows[1] = acc[1] * h3;
+        if (nk > 2) rows[2] = acc[2] * h3;
+      }
+    };
+    double r1[3], r2[3];
+    // Hpp p~ and Hkp p~
+    phi_apply_into(c0_, x);
+    phi_applyT_from(c0_, pc.data());
+    pair(1, r1);
+    for (int i = 0; i < np; i++) y[i] = (opt_.beta * pc[i] - pa[i]) * h3;
+    // Hpk k~ and Hkk k~
+    fill(c0_, 0.0);
+    set_secondary_coefficients(x[np], nk > 1 ? x[np + 1] : 0.0, nk > 2 ? x[np + 2] : 0.0);
+    pair(2, r2);
+    for (int i = 0; i < np; i++) y[i] += -h3 * pa[i];
+    for (int j = 0; j < std::min(nk, 3); j++) y[np + j] = r1[j] + r2[j];
   }
   void get_state(int i, void* out) override {
     if (!state_done_ || !full() || i < 0 || i > nt_)
@@ -1893,6 +2036,10 @@ class Engine final : public EngineBase {
   // Tumor state and work
   R *c0_ = nullptr, *ct_ = nullptr, *p0_ = nullptr, *pt_ = nullptr, *tmp_ = nullptr,
     *tmp2_ = nullptr, *d1_ = nullptr;
+  // Hessian with diffusivity inversion: k~ (DiffCoef::temp_[7]), the incremental sources' work
+  // field, the reference's p_[nt] and c_[nt] of checkpointed runs
+  R *ksec_ = nullptr, *inc_ = nullptr, *pnt_ = nullptr, *cfin_ = nullptr;
+  bool ksec_set_ = false;
   R *chat_ = nullptr, *xhat_ = nullptr, *rhat_ = nullptr, *phat_ = nullptr, *what_ = nullptr;
   R *g3s_ = nullptr, *g3r_ = nullptr, *ga3_ = nullptr;
   R* wkern_ = nullptr;

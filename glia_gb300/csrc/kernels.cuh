@@ -620,6 +620,35 @@ __global__ void __launch_bounds__(kThreads)
   if (threadIdx.x == 0) sc->red[slot] = acc[0];
 }
 
+// DiffCoef::setSecondaryCoefficients (src/mat/DiffCoef.cpp:44-58): k~ = k1 wm + k2 gm + k3 csf.
+template <typename R>
+__global__ void __launch_bounds__(kThreads)
+    k_assemble_secondary(int64_t N, R* __restrict__ out, const R* __restrict__ wm,
+                         const R* __restrict__ gm, const R* __restrict__ csf, double k1,
+                         double k2, double k3) {
+  GRID_STRIDE(i, N) {
+    R v = wm[i] * (R)k1;
+    v += (R)k2 * gm[i];
+    v += (R)k3 * csf[i];
+    out[i] = v;
+  }
+}
+
+// solveIncremental's mixture (src/pde/PdeOperators.cpp:200-220): out = 0.5 (a + b) + e, e = a
+// before the step (mode 1) or b after it (mode 2), in the reference's operation order.
+template <typename R>
+__global__ void __launch_bounds__(kThreads)
+    k_incr_mix(int64_t N, R* __restrict__ out, const R* __restrict__ a, const R* __restrict__ b,
+               int mode) {
+  const R* e = mode == 1 ? a : b;
+  GRID_STRIDE(i, N) {
+    R v = a[i] + b[i];
+    v *= (R)0.5;
+    v += e[i];
+    out[i] = v;
+  }
+}
+
 // MatProp::setValuesSinusoidal (src/mat/MatProp.cpp:34-68) and
 // DiffCoef::setValuesSinusoidal (src/mat/DiffCoef.cpp:134-187); sum of the k field.
 template <typename R>

@@ -121,6 +121,11 @@ class DiffCoef {
   PetscErrorCode setValuesSinusoidal(std::shared_ptr<Parameters>, ScalarType scale) {
     return glia_set_diffusivity_sinusoidal(spec_ops_->ctx_, scale);
   }
+  // DiffCoef::setSecondaryCoefficients (src/mat/DiffCoef.cpp:44-58), read by solveState(2)
+  PetscErrorCode setSecondaryCoefficients(ScalarType k1, ScalarType k2, ScalarType k3,
+                                          std::shared_ptr<MatProp>, std::shared_ptr<Parameters>) {
+    return glia_set_secondary_coefficients(spec_ops_->ctx_, k1, k2, k3);
+  }
   std::shared_ptr<Parameters> params_;
   std::shared_ptr<SpectralOperators> spec_ops_;
 };
@@ -261,7 +266,8 @@ class DerivativeOperatorsRD {
                                                  data->dt1().data(), J, dJ.data());
   }
   // DerivativeOperatorsRD::evaluateHessian(Vec y, Vec x) (src/grad/DerivativeOperatorsRD.cpp:
-  // 229-438), the Gauss-Newton p block, linearised at the last evaluation
+  // 229-438): the p block, or the p and kappa blocks with diffusivity inversion, linearised at
+  // the last evaluation
   PetscErrorCode evaluateHessian(Vec& y, const Vec& x) {
     int rc = sync_settings();
     y.assign(x.size(), 0.0);

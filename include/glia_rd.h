@@ -171,10 +171,17 @@ int glia_set_obs_filter(glia_ctx* ctx, const void* filter);
 /* ---- PDE operators --------------------------------------------------------------------------- */
 /* Tumor::c_0_ (used by the derivative operators when flag_reaction_inv is set). */
 int glia_set_c0(glia_ctx* ctx, const void* c0);
+/* DiffCoef::setSecondaryCoefficients (src/mat/DiffCoef.cpp:44-58): the diffusivity direction
+ * k~ = k1 wm + k2 gm + k3 csf of the incremental forward with linearized = 2 (k2, k3 from the
+ * current gm / glm ratios when nk = 1). */
+int glia_set_secondary_coefficients(glia_ctx* ctx, double k1, double k2, double k3);
 /* PdeOperatorsRD::solveState(int linearized) (src/pde/PdeOperators.cpp:235-316).
  * c0 may be NULL (use Tumor::c_0_); c1 may be NULL. linearized = 0: the state equation (fills
  * the history); 1: the incremental forward around the history of the last linearized = 0 solve,
- * the logistic step linearised at the state at each step's start (reaction(1, i), :140-190). */
+ * the logistic step linearised at the state at each step's start (reaction(1, i), :140-190);
+ * 2: as 1 plus the sources of the diffusivity direction (solveIncremental, :192-233) around each
+ * step, dt/4 div(k~ grad(0.5 (c_i + c_i+1) + c_i)) before the first diffusion half step and
+ * ... + c_i+1 after the second (needs glia_set_secondary_coefficients). */
 int glia_solve_state(glia_ctx* ctx, int linearized, const void* c0, void* c1);
 /* PdeOperatorsRD::solveAdjoint(int linearized) (src/pde/PdeOperators.cpp:372-420).
  * Needs a preceding glia_solve_state. a0 may be NULL. linearized = 1: adjoint; 2: incremental
@@ -195,13 +202,19 @@ int glia_eval_gradient(glia_ctx* ctx, const double* x, int nx, const void* d1, d
 int glia_eval_objective_and_gradient(glia_ctx* ctx, const double* x, int nx, const void* d1,
                                      double* J, double* dJ);
 /* DerivativeOperatorsRD::evaluateHessian (src/grad/DerivativeOperatorsRD.cpp:229-438): the
- * Gauss-Newton matvec y = H x of the p block (the branch without diffusivity inversion,
- * :398-425): c~0 = Phi x, incremental forward (glia_solve_state 1), p~_t = -O^T O c~(1),
- * incremental adjoint (glia_solve_adjoint 2), y = h^3 (beta Phi^T c~0 - Phi^T a~0), or
- * beta x - h^3 Phi^T a~0 with the L2b regulariser. Linearised at the state history of the last
- * gradient evaluation or state solve (so call it after glia_eval_* at the current iterate).
- * x and y have nx = np + nk + nr entries (host doubles); entries past np are beta x (L2b) or 0.
- * GLIA_ERR_INVALID when diffusivity_inversion is set (the kappa blocks are not provided). */
+ * Gauss-Newton matvec y = H x, linearised at the state history of the last gradient evaluation
+ * or state solve (so call it after glia_eval_* at the current iterate). x and y have
+ * nx = np + nk + nr entries (host doubles).
+ * Without diffusivity inversion (:398-425), the p block: c~0 = Phi x, incremental forward
+ * (glia_solve_state 1), p~_t = -O^T O c~(1), incremental adjoint (glia_solve_adjoint 2),
+ * y = h^3 (beta Phi^T c~0 - Phi^T a~0), or beta x - h^3 Phi^T a~0 with the L2b regulariser;
+ * entries past np are beta x (L2b) or 0.
+ * With diffusivity inversion (:244-397), the p and kappa blocks [Hpp p~ + Hpk k~;
+ * Hkp p~ + Hkk k~]: a second incremental pair from c~0 = 0 with k~ = x's kappa entries
+ * (glia_set_secondary_coefficients, glia_solve_state 2); the kappa rows integrate
+ * grad c . grad a~ in time like the gradient, where the t = 1 term reads p_[nt] as the reference
+ * leaves it: the final condition of the last linearized = 1 adjoint (0 before the first). The
+ * p rows use the L2 form. Rows past np + nk (rho) are 0. */
 int glia_hessian_matvec(glia_ctx* ctx, const double* x, int nx, double* y);
 
 int glia_get_stats(const glia_ctx* ctx, glia_stats* st);

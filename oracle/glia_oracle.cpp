@@ -271,6 +271,8 @@ struct Ctx {
   // PdeOperatorsRD history
   std::vector<Field> c_hist, p_hist, c_half;
   bool state_done = false;
+  // DiffCoef::temp_[7]: sum_i m_i k~_i of the Hessian's diffusivity direction
+  Field ksec;
   // scratch
   std::vector<cplx> xh, wh;
   Field d1;
@@ -350,6 +352,33 @@ struct Ctx {
       t[1][i] = kxx[i] * t[4][i];
       t[2][i] = kxx[i] * t[5][i];
       t[3][i] = kxx[i] * t[6][i];
+    }
+    divergence(dc, t[1].data(), t[2].data(), t[3].data(), t[7].data());
+  }
+  // DiffCoef::setSecondaryCoefficients (src/mat/DiffCoef.cpp:44-58): k~ = k1 wm + k2 gm + k3 csf,
+  // with k2, k3 from the current ratios when nk = 1
+  void setSecondaryCoefficients(double k1, double k2, double k3) {
+    if (opt.nk == 1) {
+      k2 = k_gm_wm * k1;
+      k3 = k_glm_wm * k1;
+    }
+    ksec.assign(N, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; i++) {
+      double v = wm[i] * k1;
+      v += k2 * gm[i];
+      v += k3 * csf[i];
+      ksec[i] = v;
+    }
+  }
+  // DiffCoef::applyDWithSecondaryCoeffs (:273-300): dc = div(k~ grad c); dc may alias c
+  void applyDsec(double* dc, const double* c) {
+    gradient(t[4].data(), t[5].data(), t[6].data(), c);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; i++) {
+      t[1][i] = ksec[i] * t[4][i];
+      t[2][i] = ksec[i] * t[5][i];
+      t[3][i] = ksec[i] * t[6][i];
     }
     divergence(dc, t[1].data(), t[2].data(), t[3].data(), t[7].data());
   }
@@ -726,11 +755,34 @@ struct Ctx {
   }
 
   // ---- PdeOperatorsRD (src/pde/PdeOperators.cpp) ----
+  // solveIncremental (:192-233): c~ += dts / 2 * D~(0.5 (c_i + c_i+1) + c_i) before the step
+  // (mode 1) or ... + c_i+1 after it (mode 2); dts is the half step the caller passes
+  void solveIncremental(double* ctil, double dts, int iter, int mode) {
+    Field temp(N);
+    const double* a = c_hist[iter].data();
+    const double* b = c_hist[iter + 1].data();
+    const double* e = mode == 1 ? a : b;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; i++) {
+      double v = a[i] + b[i];
+      v *= 0.5;
+      v += e[i];
+      temp[i] = v;
+    }
+    applyDsec(temp.data(), temp.data());
+    vaxpy(ctil, dts / 2, temp.data(), N);
+  }
   // linearized = 0 fills the history; linearized = 1 is the incremental forward around it, the
-  // reaction linearised at c_[i] (reaction(1, i) reads c_[iter], :153-156), history untouched.
+  // reaction linearised at c_[i] (reaction(1, i) reads c_[iter], :153-156), history untouched;
+  // linearized = 2 adds the diffusivity direction's source terms (solveIncremental) around each
+  // step, before the first and after the second diffusion half step.
   int solveState(int linearized) {
     if (linearized != 0 && (!state_done || (int)c_hist.size() != nt + 1)) {
       err = "solveState(1) needs a preceding solveState(0)";
+      return GLIA_ERR_STATE;
+    }
+    if (linearized == 2 && (int64_t)ksec.size() != N) {
+      err = "solveState(2) needs the secondary diffusion coefficients";
       return GLIA_ERR_STATE;
     }
     st.nb_state_solves++;
@@ -743,6 +795,7 @@ struct Ctx {
     st.diff_ksp_itr_state = 0;
     for (int i = 0; i < nt; i++) {
       int rc;
+      if (linearized == 2) solveIncremental(ct.data(), dt / 2, i, 1);
       if (order == 2) {
         if ((rc = solve(ct.data(), dt / 2.0))) return rc;
         st.diff_ksp_itr_state += ksp_itr;
@@ -750,6 +803,7 @@ struct Ctx {
         reaction(ct.data(), c_hist[i].data(), linearized);
         if ((rc = solve(ct.data(), dt / 2.0))) return rc;
         st.diff_ksp_itr_state += ksp_itr;
+        if (linearized == 2) solveIncremental(ct.data(), dt / 2, i, 2);
       } else {
         if ((rc = solve(ct.data(), dt))) return rc;
         st.diff_ksp_itr_state += ksp_itr;
@@ -782,7 +836,9 @@ struct Ctx {
     }
     st.nb_adjoint_solves++;
     vcopy(p0.data(), pt.data(), N);
-    p_hist.assign(nt + 1, Field());
+    // the history vectors live as long as nt does (resizeTimeHistory, :49-103, VecSet to 0);
+    // p_[nt] changes only in a linearized = 1 sweep
+    if ((int)p_hist.size() != nt + 1) p_hist.assign(nt + 1, Field(N, 0.0));
     if (linearized == 1) p_hist[nt] = p0;
     st.diff_ksp_itr_adj = 0;
     for (int i = 0; i < nt; i++) {
@@ -803,13 +859,58 @@ struct Ctx {
     return 0;
   }
 
-  // evaluateHessian (src/grad/DerivativeOperatorsRD.cpp:229-438), branch without diffusivity
-  // inversion (:398-425): Gauss-Newton matvec of the p block around the current history.
+  // evaluateHessian with diffusivity inversion (src/grad/DerivativeOperatorsRD.cpp:244-397):
+  // [Hpp p~ + Hpk k~; Hkp p~ + Hkk k~], each block from its own incremental forward / adjoint
+  // pair. The kappa rows are the time integral of grad c_i . grad a~_i over the stored histories,
+  // where p_[nt] is the final condition of the last linearized = 1 adjoint (solveAdjoint(2) does
+  // not write it). Rows past np + nk (rho) are 0: the reference leaves them as the caller's y.
+  int hessianDiffusivity(const double* x, double* y) {
+    const int np_ = opt.np, nk = opt.nk;
+    std::fill(y, y + nx(), 0.0);
+    auto incremental_pair = [&](int lin) -> int {
+      int rc = solveState(lin);
+      if (rc) return rc;
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < N; i++) pt[i] = -(obs_filter[i] * (obs_filter[i] * ct[i]));
+      return solveAdjoint(2);
+    };
+    auto kappa_rows = [&](bool add) {
+      Field T(N, 0.0);
+      kappaIntegral(T);
+      const double v = vdot(wm.data(), T.data(), N) * h3;
+      y[np_] = add ? y[np_] + v : v;
+      if (nk == 1) y[np_] += vdot(gm.data(), T.data(), N) * h3 * k_gm_wm;
+      if (nk > 1) y[np_ + 1] += vdot(gm.data(), T.data(), N) * h3;
+      if (nk > 2) y[np_ + 2] += vdot(csf.data(), T.data(), N) * h3;
+    };
+    std::vector<double> pa(std::max(np_, 1));
+    // Hpp p~ (:253-268): c~0 = Phi p~
+    phi_apply(c0.data(), x);
+    int rc = incremental_pair(1);
+    if (rc) return rc;
+    phi_applyT(pa.data(), p0.data());
+    phi_applyT(y, c0.data());
+    for (int i = 0; i < np_; i++) y[i] = (opt.beta * y[i] - pa[i]) * h3;
+    // Hkp p~ (:270-316)
+    kappa_rows(false);
+    // Hpk k~ (:318-349): c~0 = 0, k~ from x's kappa entries, solveState(2)
+    std::fill(c0.begin(), c0.end(), 0.0);
+    setSecondaryCoefficients(x[np_], nk > 1 ? x[np_ + 1] : 0.0, nk > 2 ? x[np_ + 2] : 0.0);
+    if ((rc = incremental_pair(2))) return rc;
+    phi_applyT(pa.data(), p0.data());
+    for (int i = 0; i < np_; i++) y[i] += -h3 * pa[i];
+    // Hkk k~ (:351-397)
+    kappa_rows(true);
+    return 0;
+  }
+  // evaluateHessian (src/grad/DerivativeOperatorsRD.cpp:229-438); without diffusivity inversion
+  // (:398-425) the Gauss-Newton matvec of the p block around the current history.
   int hessian(const double* x, double* y) {
-    if (opt.diffusivity_inversion) {
-      err = "evaluateHessian: only the p block (no diffusivity inversion) is supported";
-      return GLIA_ERR_INVALID;
+    if (!state_done) {
+      err = "evaluateHessian needs a preceding state solve or gradient";
+      return GLIA_ERR_STATE;
     }
+    if (opt.diffusivity_inversion) return hessianDiffusivity(x, y);
     const int np_ = opt.np;
     phi_apply(c0.data(), x);
     int rc = solveState(1);
@@ -859,7 +960,16 @@ struct Ctx {
   void gradDiffusion(double* dJ) {
     if (!update_kappa()) return;
     const int np_ = opt.np, nk = opt.nk;
-    Field T(N, 0.0), g1(N), g2(N), g3(N), a1(N), a2(N), a3(N);
+    Field T(N, 0.0);
+    kappaIntegral(T);
+    dJ[np_] = vdot(wm.data(), T.data(), N) * h3;
+    if (nk == 1) dJ[np_] += vdot(gm.data(), T.data(), N) * h3 * k_gm_wm;
+    if (nk > 1) dJ[np_ + 1] = vdot(gm.data(), T.data(), N) * h3;
+    if (nk > 2) dJ[np_ + 2] = vdot(csf.data(), T.data(), N) * h3;
+  }
+  // T = sum_i w_i dt grad c_i . grad p_i over the histories (trapezoid, w = 1/2 at the ends)
+  void kappaIntegral(Field& T) {
+    Field g1(N), g2(N), g3(N), a1(N), a2(N), a3(N);
     for (int i = 0; i < nt + 1; i++) {
       double wgt = (i == 0 || i == nt) ? 0.5 : 1.0;
       gradient(g1.data(), g2.data(), g3.data(), c_hist[i].data());
@@ -873,10 +983,6 @@ struct Ctx {
         T[j] += s * v;
       }
     }
-    dJ[np_] = vdot(wm.data(), T.data(), N) * h3;
-    if (nk == 1) dJ[np_] += vdot(gm.data(), T.data(), N) * h3 * k_gm_wm;
-    if (nk > 1) dJ[np_ + 1] = vdot(gm.data(), T.data(), N) * h3;
-    if (nk > 2) dJ[np_ + 2] = vdot(csf.data(), T.data(), N) * h3;
   }
   // gradReaction (:258-321)
   void gradReaction(double* dJ) {
@@ -1098,8 +1204,13 @@ int oracle_glia_set_c0(glia_ctx* ctx, const double* c0) {
   std::copy(c0, c0 + ctx->N, ctx->c0.begin());
   return GLIA_OK;
 }
+int oracle_glia_set_secondary_coefficients(glia_ctx* ctx, double k1, double k2, double k3) {
+  if (!ctx) return GLIA_ERR_INVALID;
+  ctx->setSecondaryCoefficients(k1, k2, k3);
+  return GLIA_OK;
+}
 int oracle_glia_solve_state(glia_ctx* ctx, int linearized, const double* c0, double* c1) {
-  if (!ctx || (linearized != 0 && linearized != 1)) return GLIA_ERR_INVALID;
+  if (!ctx || linearized < 0 || linearized > 2) return GLIA_ERR_INVALID;
   if (c0) std::copy(c0, c0 + ctx->N, ctx->c0.begin());
   int rc = ctx->solveState(linearized);
   if (rc) return rc;
