@@ -14,6 +14,7 @@ The default batch: 32 problems, 16 at 64^3, 12 at 128^3 and 4 at 256^3; problem 
 FP32 fields with FP64 reductions.
 
     python -m glia_gb300.batch            # autotuned batch vs the same problems one at a time
+    torchrun --nproc-per-node N -m glia_gb300.batch   # the batch split over N GPUs (LPT by n^3 nt)
 """
 from __future__ import annotations
 
@@ -129,6 +130,49 @@ def longest_first(problems):
     return sorted(range(len(problems)), key=lambda i: -problems[i].n ** 3)
 
 
+def cost(problem) -> float:
+    """Estimated work of one gradient evaluation, n^3 nt (the PCG iterations per solve of this
+    problem family vary little with the parameters)."""
+    return float(problem.n) ** 3 * problem.nt
+
+
+def lpt_partition(costs, world: int):
+    """Greedy longest-processing-time assignment of problems to ranks: problems by decreasing
+    cost, each to the least-loaded rank (ties to the lower rank, then the lower index), so the
+    largest rank load is at most 4/3 of the optimum. One index list per rank, each by decreasing
+    cost."""
+    if world < 1:
+        raise ValueError("world size must be at least 1")
+    order = sorted(range(len(costs)), key=lambda i: (-costs[i], i))
+    loads = [0.0] * world
+    parts = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda q: (loads[q], q))
+        parts[r].append(i)
+        loads[r] += costs[i]
+    return parts
+
+
+def evaluate_sharded(problems, evaluate_one, rank: int, world: int):
+    """Multi-GPU batch: this rank evaluates its LPT share (evaluate_one(i) -> (J, dJ), on the
+    rank's own GPU), then one all_gather_object gives every rank every problem's (J, dJ). The
+    evaluations need no collective; the gather is the only exchange. Returns (results in problem
+    order, the partition)."""
+    parts = lpt_partition([cost(p) for p in problems], world)
+    mine = {i: evaluate_one(i) for i in parts[rank]}
+    gathered = [mine]
+    if world > 1:
+        import torch.distributed as dist
+
+        gathered = [None] * world
+        dist.all_gather_object(gathered, mine)
+    out = [None] * len(problems)
+    for part in gathered:
+        for i, r in part.items():
+            out[i] = r
+    return out, parts
+
+
 def autotune(problems, nt_probe: int = 10, cache: str = CACHE, force: bool = False) -> dict:
     """Chooses concurrency and per-size launch geometry by timing a shortened copy of the batch
     (nt_probe steps); caches the choice per batch signature."""
@@ -179,8 +223,45 @@ def run(nt: int = 100, repeats: int = 2):
             "speedup": t_seq / t_bat, "schedule": choice}
 
 
+def run_distributed(nt: int = 100):
+    """The default batch over WORLD_SIZE ranks (torchrun, one GPU per rank): each rank builds
+    contexts for its LPT share on its GPU and evaluates them with the autotuned schedule; rank 0
+    reports the slowest rank's wall time and the gathered results' count."""
+    import torch
+    import torch.distributed as dist
+
+    rank, world = int(os.environ["RANK"]), int(os.environ["WORLD_SIZE"])
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
+    dist.init_process_group("nccl")
+    problems = default_batch(nt)
+    parts = lpt_partition([cost(p) for p in problems], world)
+    share = [problems[i] for i in parts[rank]]
+    choice = autotune(share) if share else {"concurrency": 1, "geometry": {}}
+    batch = Batch(share)
+    batch.set_geometry(choice["geometry"])
+    local = {i: k for k, i in enumerate(parts[rank])}
+    dist.barrier()
+    t0 = time.perf_counter()
+    _, res = batch.evaluate(choice["concurrency"])
+    results, _ = evaluate_sharded(problems, lambda i: res[local[i]], rank, world)
+    dist.barrier()
+    dt = torch.tensor([time.perf_counter() - t0], dtype=torch.float64, device="cuda")
+    dist.all_reduce(dt, op=dist.ReduceOp.MAX)
+    batch.close()
+    out = {"problems": signature(problems), "ranks": world, "wall_s": float(dt.item()),
+           "evals_per_s": len(problems) / float(dt.item()), "gathered": sum(
+               r is not None for r in results), "partition": parts}
+    dist.destroy_process_group()
+    return out if rank == 0 else None
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--nt", type=int, default=100)
     a = ap.parse_args()
-    print(json.dumps(run(a.nt)))
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        r = run_distributed(a.nt)
+        if r is not None:
+            print(json.dumps(r))
+    else:
+        print(json.dumps(run(a.nt)))
