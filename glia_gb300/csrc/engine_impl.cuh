@@ -23,6 +23,7 @@
 #include "engine.hpp"
 #include "kernels.cuh"
 #include "ktimer.cuh"
+#include "zpass2.cuh"
 #include "zpass.cuh"
 #include "ownfft.cuh"
 
@@ -460,6 +461,9 @@ class Engine final : public EngineBase {
       if (which == 0)
         k_yinv<NN><<<std::min(own_res_[0], pw_blocks_), 256, yinv_smem_bytes<NN>(), stream_>>>(
             g3r_, g3s_, tw256_);
+      else if (which == 1 && zpass2_)
+        k_zpass2<NN><<<std::min(own_res_[1], pw_blocks_), 256, zpass2_smem_bytes<NN>(),
+                       stream_>>>(g3s_, kxx_, tw256_);
       else if (which == 1)
         k_zpass<NN><<<std::min(own_res_[1], pw_blocks_), 256, zpass_smem_bytes<NN>(), stream_>>>(
             g3s_, kxx_, tw256_);
@@ -497,7 +501,12 @@ class Engine final : public EngineBase {
                                      per_sm(k_xfwd_own<NN, EPI_SETUP>, fs),
                                      per_sm(k_xfwd_own<NN, EPI_CGW>, fs)});
         own_res_[0] = sms_ * per_sm(k_yinv<NN>, yinv_smem_bytes<NN>());
-        own_res_[1] = sms_ * per_sm(k_zpass<NN>, zpass_smem_bytes<NN>());
+        // z pass: two real lines per complex transform (k_zpass2) unless GLIA_ZPASS2=0 picks
+        // the even/odd half-length version (k_zpass)
+        const char* z2 = std::getenv("GLIA_ZPASS2");
+        zpass2_ = !(z2 && z2[0] == '0');
+        own_res_[1] = sms_ * (zpass2_ ? per_sm(k_zpass2<NN>, zpass2_smem_bytes<NN>())
+                                      : per_sm(k_zpass<NN>, zpass_smem_bytes<NN>()));
         const char* te = std::getenv("GLIA_TMA");
         tma_ = te && te[0] == '1';
         own_res_[2] = sms_ * (tma_ ? per_sm(k_yfwd_tma<NN>, yfwd_tma_smem_bytes<NN>())
@@ -2003,6 +2012,7 @@ class Engine final : public EngineBase {
   int own_res_[3] = {0, 0, 0};       // ... of k_yinv, k_zpass, k_yfwd
   CUtensorMap kmap_{};               // TMA map of the packed line arrays (k_yfwd)
   bool tma_ = false;                 // k_yfwd stages with TMA copies (GLIA_TMA=1)
+  bool zpass2_ = true;               // z pass with two real lines per complex transform
   bool own_ = false;  // own y and z passes (x pass on): no cuFFT inside the D apply
   float2* tw_ = nullptr;
   char* fft_ws_ = nullptr;
