@@ -361,8 +361,9 @@ class Engine final : public EngineBase {
 
   // First half of a spectral D apply, from the spectrum src (plain) or from the new PCG direction
   // p = P r + b p (CGDIR: src = r, pdir = p), up to the spectra of k grad u that d_back
-  // diverges. Own transforms (default, FP32, n = 64 ... 256): k_xinv -> G in g3r_, k_yinv ->
-  // packed lines in g3s_, k_zpass (k multiplied there, in place), k_yfwd -> M in g3r_. "2d": the
+  // diverges. Own transforms (default, FP32, n = 64 ... 256): k_xinv -> G in g3r_, k_yinv_bulk
+  // (or k_yinv) -> packed lines in g3s_, k_zpass2 (or k_zpass; k multiplied there, in place),
+  // k_yfwd -> M in g3r_. "2d": the
   // x pass writes (x, ky, kz) per component to g3s_ and cuFFT does batched 2-D (y, z)
   // transforms around k_mul_k3. Otherwise g3s_ holds the full 3-D spectra.
   template <bool CGDIR>
@@ -453,12 +454,15 @@ class Engine final : public EngineBase {
       else xfwd_n<64, EPI, false>(g3s_, aux_in, cx, out, aux_out, scale, blocks);
     }
   }
-  // own y / z passes: 0 = k_yinv (g3r_ -> g3s_), 1 = k_zpass (g3s_ in place, k), 2 = k_yfwd
+  // own y / z passes: 0 = y inverse (g3r_ -> g3s_), 1 = z pass (g3s_ in place, k), 2 = k_yfwd
   // (g3s_ -> g3r_)
   template <int NN>
   void own_n(int which) {
     if constexpr (std::is_same<R, float>::value) {
-      if (which == 0)
+      if (which == 0 && yinv_bulk_)
+        k_yinv_bulk<NN><<<std::min(own_res_[0], pw_blocks_), 256, yinv_bulk_smem_bytes<NN>(),
+                          stream_>>>(g3r_, g3s_, tw256_, sc_);
+      else if (which == 0)
         k_yinv<NN><<<std::min(own_res_[0], pw_blocks_), 256, yinv_smem_bytes<NN>(), stream_>>>(
             g3r_, g3s_, tw256_);
       else if (which == 1 && zpass2_)
@@ -500,7 +504,12 @@ class Engine final : public EngineBase {
         xres_fwd_ = sms_ * std::min({per_sm(k_xfwd_own<NN, EPI_APPLYD>, fs),
                                      per_sm(k_xfwd_own<NN, EPI_SETUP>, fs),
                                      per_sm(k_xfwd_own<NN, EPI_CGW>, fs)});
-        own_res_[0] = sms_ * per_sm(k_yinv<NN>, yinv_smem_bytes<NN>());
+        // y-inverse rows staged by bulk copies (default) or per-thread cp.async
+        // (GLIA_YINV_BULK=0)
+        const char* yb = std::getenv("GLIA_YINV_BULK");
+        yinv_bulk_ = !(yb && yb[0] == '0');
+        own_res_[0] = sms_ * (yinv_bulk_ ? per_sm(k_yinv_bulk<NN>, yinv_bulk_smem_bytes<NN>())
+                                         : per_sm(k_yinv<NN>, yinv_smem_bytes<NN>()));
         // z pass: two real lines per complex transform (k_zpass2) unless GLIA_ZPASS2=0 picks
         // the even/odd half-length version (k_zpass)
         const char* z2 = std::getenv("GLIA_ZPASS2");
@@ -2013,6 +2022,7 @@ class Engine final : public EngineBase {
   CUtensorMap kmap_{};               // TMA map of the packed line arrays (k_yfwd)
   bool tma_ = false;                 // k_yfwd stages with TMA copies (GLIA_TMA=1)
   bool zpass2_ = true;               // z pass with two real lines per complex transform
+  bool yinv_bulk_ = true;            // y-inverse rows staged by bulk copies
   bool own_ = false;  // own y and z passes (x pass on): no cuFFT inside the D apply
   float2* tw_ = nullptr;
   char* fft_ws_ = nullptr;

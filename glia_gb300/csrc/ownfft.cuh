@@ -164,6 +164,126 @@ __global__ void __launch_bounds__(256, 2)
 }
 
 template <int NN>
+constexpr int yinv_bulk_smem_bytes() {
+  return yinv_smem_bytes<NN>() + 2 * (int)sizeof(uint64_t);
+}
+
+// k_yinv with the input rows staged by bulk copies (the copy engine, one 16-byte aligned window of
+// T + 2 complex per row and thread, completing on one mbarrier per slot) instead of per-thread
+// 16-byte cp.async chunks; the kz = n/2 column still by cp.async. The windows cross 128-byte
+// lines (rows are n/2 + 1 complex long), which costs the load/store unit extra wavefronts per
+// cp.async chunk. Waits are bounded; a timeout records DevScalars::dev_fault.
+template <int NN>
+__global__ void __launch_bounds__(256, 2)
+    k_yinv_bulk(const float* __restrict__ Gin, float* __restrict__ Hout,
+                const float2* __restrict__ tw_g, DevScalars* __restrict__ sc) {
+  using D = YDecomp<NN>;
+  constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T, NB1 = R2 / GR;
+  constexpr int NQ = NN / 2, NH = NN / 2 + 1, CB = NQ / T;
+  constexpr int PS = NN * NH, NS = NN * PS, NP = NN * NN * NQ;
+  constexpr int ntiles = NN * CB, TS = T + 2;
+  constexpr unsigned SLOT_BYTES = NN * TS * sizeof(float2);
+  extern __shared__ float4 yinv_dyn[];
+  float2* slGx = reinterpret_cast<float2*>(yinv_dyn);
+  float2* slG0 = slGx + NN * TS;
+  float2* nyq = slG0 + NN * TS;
+  float2* sm = nyq + 2 * NN;
+  float2* tw = sm + NN * T;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tw + 256);
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_mbar_init();
+  }
+  fill_twb<D, +1>(tw, tw_g);
+  __syncthreads();
+  const int c = threadIdx.x % T, gi = threadIdx.x / T;
+  const float2* Gx = reinterpret_cast<const float2*>(Gin);
+  const float2* G0 = Gx + NS;
+  float2* H = reinterpret_cast<float2*>(Hout);
+  // after a CTA barrier that ends every read of the slot: rows by bulk copies, nyq by cp.async
+  auto stage = [&](float2* slot, float2* ny, const float2* G, int t, uint64_t* bar) {
+    if (t < ntiles) {
+      const int x = t / CB, cb = t - x * CB;
+      if (threadIdx.x == 0) mbar_arrive_expect_tx(bar, SLOT_BYTES);
+      if ((int)threadIdx.x < NN) {
+        const int r = threadIdx.x;
+        fence_proxy_async();
+        bulk_load(slot + r * TS, G + x * PS + r * NH + cb * T - (r & 1),
+                  TS * (unsigned)sizeof(float2), bar);
+        if (cb == 0) cp_async8(ny + r, G + x * PS + r * NH + NQ);
+      }
+    }
+    cp_async_commit();
+  };
+  // the slot's rows have landed (uniform result); on a timeout record the fault and wait, bounded,
+  // for the other slot's copies
+  auto ready = [&](int which, int it) {
+    const bool ok = threadIdx.x != 0 || mbar_wait(&bars[which], (unsigned)(it & 1));
+    if (!__syncthreads_or(!ok)) return true;
+    if (threadIdx.x == 0) {
+      atomicExch(&sc->dev_fault, 1);
+      mbar_wait(&bars[which ^ 1], (unsigned)(it & 1));
+    }
+    cp_async_wait<0>();
+    __syncthreads();
+    return false;
+  };
+  stage(slGx, nyq, Gx, blockIdx.x, &bars[0]);
+  stage(slG0, nyq + NN, G0, blockIdx.x, &bars[1]);
+  int it = 0;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, it++) {
+    const int x = tile / CB, kz = (tile - x * CB) * T + c;
+    const bool pk = kz == 0;
+    cp_async_wait<1>();  // nyq of G_x
+    if (!ready(0, it)) return;
+    xdft<D, +1>(
+        sm, tw, c, gi,
+        [&](int, int b, int a) {
+          const int ky = R2 * a + b;
+          float2 v = slGx[ky * TS + (ky & 1) + c];
+          if (pk) {
+            const float2 w = nyq[ky];
+            v = make_float2(v.x - w.y, v.y + w.x);
+          }
+          return v;
+        },
+        [&] { stage(slGx, nyq, Gx, tile + gridDim.x, &bars[0]); },
+        [&](int, int k1, int k2, float2 y) { H[(x * NN + k1 + R1 * k2) * NQ + kz] = y; });
+    cp_async_wait<1>();  // nyq of G_0
+    if (!ready(1, it)) return;
+    float2 v[NB1][R1];
+#pragma unroll
+    for (int m = 0; m < NB1; m++) {
+      const int b = gi + GR * m;
+#pragma unroll
+      for (int a = 0; a < R1; a++) {
+        const int ky = R2 * a + b;
+        float2 val = slG0[ky * TS + (ky & 1) + c];
+        if (pk) {
+          const float2 w = nyq[NN + ky];
+          val = make_float2(val.x - w.y, val.y + w.x);
+        }
+        v[m][a] = val;
+      }
+    }
+    __syncthreads();
+    stage(slG0, nyq + NN, G0, tile + gridDim.x, &bars[1]);
+    xdft<D, +1>(
+        sm, tw, c, gi, [&](int m, int, int a) { return v[m][a]; }, [] {},
+        [&](int, int k1, int k2, float2 y) { H[2 * NP + (x * NN + k1 + R1 * k2) * NQ + kz] = y; });
+    xdft<D, +1>(
+        sm, tw, c, gi,
+        [&](int m, int b, int a) {
+          const float w = (float)wavenum(R2 * a + b, NN);
+          return make_float2(-w * v[m][a].y, w * v[m][a].x);
+        },
+        [] {}, [&](int, int k1, int k2, float2 y) { H[NP + (x * NN + k1 + R1 * k2) * NQ + kz] = y; });
+  }
+  cp_async_wait<0>();
+}
+
+template <int NN>
 constexpr int yfwd_smem_bytes() {
   return (3 * NN * YDecomp<NN>::T + 2 * NN + 256) * (int)sizeof(float2);
 }

@@ -61,6 +61,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
+// bytes (a multiple of 16) from global src to shared dst, both 16-byte aligned, completing on bar
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes,
+                                          uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // One CTA waits on an mbarrier that nothing signals: the bounded wait must give up and record
 // the fault (glia_selftest_bounded_wait).
 static __global__ void k_selftest_wait(int* fault) {

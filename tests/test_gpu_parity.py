@@ -273,13 +273,13 @@ def test_repeated_adjoint_after_one_state_solve_checkpointed():
     assert rel_l2(a, f.solve_adjoint(pt)) < 1e-12
 
 
-@pytest.mark.parametrize("path", ["own", "own_tma", "own_evenodd", "2d"])
+@pytest.mark.parametrize("path", ["own", "own_tma", "own_evenodd", "own_yinv_cpasync", "2d"])
 @pytest.mark.parametrize("n", [64, 128, 256])
 def test_transform_paths_match_cufft_3d(n, path, monkeypatch):
     """FP32 D apply, state solve and gradient through the library's own x / y / z transform
-    kernels ("own": k_xinv, k_yinv, k_zpass2, k_yfwd, k_xfwd; "own_evenodd": the even/odd z pass
-    k_zpass) and through the x pass around batched 2-D cuFFT ("2d"), against the batched 3-D
-    cuFFT path."""
+    kernels ("own": k_xinv, k_yinv_bulk, k_zpass2, k_yfwd, k_xfwd; "own_evenodd": the even/odd
+    z pass k_zpass; "own_yinv_cpasync": k_yinv) and through the x pass around batched 2-D cuFFT
+    ("2d"), against the batched 3-D cuFFT path."""
     nt = 3
     wl, tissue, centers = small_problem(n, nt, n_gauss=8)
     d1 = observation(wl, tissue, centers)
@@ -290,6 +290,8 @@ def test_transform_paths_match_cufft_3d(n, path, monkeypatch):
         monkeypatch.setenv("GLIA_TMA", "1")
     if path == "own_evenodd":
         monkeypatch.setenv("GLIA_ZPASS2", "0")
+    if path == "own_yinv_cpasync":  # y-inverse rows staged by per-thread cp.async
+        monkeypatch.setenv("GLIA_YINV_BULK", "0")
     for on in (path, "0"):
         monkeypatch.setenv("GLIA_XPASS", on)
         g = gpu(n, MIXED)
