@@ -39,8 +39,8 @@ enum KSlot {
   KS_XFWD_SETUP,         // k_xfwd<EPI_SETUP>: forward x transforms, divergence, solve set-up
   KS_XFWD_CGW,           // k_xfwd<EPI_CGW>: forward x transforms, divergence, w = A p
   KS_XFWD_APPLYD,        // k_xfwd<EPI_APPLYD>: forward x transforms, divergence, D u
-  KS_YINV,               // k_yinv: inverse y transforms (packed kz = 0 / n/2 column)
-  KS_ZFUSED,             // k_zpass: z C2R, k multiply, z R2C per line
+  KS_YINV,               // k_yinv_bulk (or k_yinv): inverse y transforms, packed kz = 0 / n/2
+  KS_ZFUSED,             // k_zpass2 (or k_zpass): z C2R, k multiply, z R2C per line
   KS_YFWD,               // k_yfwd: forward y transforms, unpacking
   KS_COUNT
 };
@@ -52,7 +52,7 @@ static const char* const kSlotNames[KS_COUNT] = {
     "copy_d2d",           "cufft_r2c",      "cufft_c2r",       "cufft_r2c_x3",
     "cufft_c2r_x3",       "ref_vector_ops", "ref_dot",         "k_zpass_mulk",
     "cufft_c2c_2d",       "k_xinv",         "k_xfwd_setup",    "k_xfwd_cgw",
-    "k_xfwd_applyd",      "k_yinv",         "k_zpass",         "k_yfwd"};
+    "k_xfwd_applyd",      "k_yinv_bulk",    "k_zpass2",         "k_yfwd"};
 
 struct KTimer {
   bool on = false;
