@@ -113,6 +113,9 @@ SIGNATURES = {
     "phi_apply_transpose": (c_int, [_CTX, _P, _D]),
     "set_obs_threshold": (c_int, [_CTX, _P, c_double]),
     "set_obs_filter": (c_int, [_CTX, _P]),
+    "set_obs_threshold0": (c_int, [_CTX, _P, c_double]),
+    "set_obs_filter0": (c_int, [_CTX, _P]),
+    "set_data0": (c_int, [_CTX, _P]),
     "set_c0": (c_int, [_CTX, _P]),
     "set_secondary_coefficients": (c_int, [_CTX, c_double, c_double, c_double]),
     "solve_state": (c_int, [_CTX, c_int, _P, _P]),

@@ -165,6 +165,31 @@ class Context:
         finally:
             self._keep = []
 
+    def set_obs_threshold0(self, data, thr):
+        """Observation operator at t = 0 of the two-snapshot objective: [data > thr]."""
+        self._keep = []
+        try:
+            self._check(self.api.set_obs_threshold0(self._h, self._field_in(data), thr),
+                        "set_obs_threshold0")
+        finally:
+            self._keep = []
+
+    def set_obs_filter0(self, f):
+        self._keep = []
+        try:
+            self._check(self.api.set_obs_filter0(self._h, self._field_in(f)), "set_obs_filter0")
+        finally:
+            self._keep = []
+
+    def set_data0(self, d0):
+        """Data at t = 0 (two-snapshot objective); None returns to one snapshot."""
+        self._keep = []
+        try:
+            p = None if d0 is None else self._field_in(d0)
+            self._check(self.api.set_data0(self._h, p), "set_data0")
+        finally:
+            self._keep = []
+
     def set_c0(self, c0):
         self._keep = []
         try:

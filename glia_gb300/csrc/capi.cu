@@ -214,6 +214,17 @@ int glia_set_obs_filter(glia_ctx* ctx, const void* f) {
   if (!f) return GLIA_ERR_INVALID;
   return guarded(ctx, [&](glia::EngineBase& e) { e.set_obs_filter(f); });
 }
+int glia_set_obs_threshold0(glia_ctx* ctx, const void* data, double thr) {
+  if (!data) return GLIA_ERR_INVALID;
+  return guarded(ctx, [&](glia::EngineBase& e) { e.set_obs_threshold0(data, thr); });
+}
+int glia_set_obs_filter0(glia_ctx* ctx, const void* f) {
+  if (!f) return GLIA_ERR_INVALID;
+  return guarded(ctx, [&](glia::EngineBase& e) { e.set_obs_filter0(f); });
+}
+int glia_set_data0(glia_ctx* ctx, const void* d0) {
+  return guarded(ctx, [&](glia::EngineBase& e) { e.set_data0(d0); });
+}
 int glia_set_c0(glia_ctx* ctx, const void* c0) {
   if (!c0) return GLIA_ERR_INVALID;
   return guarded(ctx, [&](glia::EngineBase& e) { e.set_c0(c0); });

@@ -34,6 +34,9 @@ class EngineBase {
   virtual void phi_apply_transpose(const void* v, double* pout) = 0;
   virtual void set_obs_threshold(const void* data, double thr) = 0;
   virtual void set_obs_filter(const void* f) = 0;
+  virtual void set_obs_threshold0(const void* data, double thr) = 0;
+  virtual void set_obs_filter0(const void* f) = 0;
+  virtual void set_data0(const void* d0) = 0;
   virtual void set_c0(const void* c0) = 0;
   virtual void set_secondary_coefficients(double k1, double k2, double k3) = 0;
   virtual void solve_state(int linearized, const void* c0, void* c1) = 0;

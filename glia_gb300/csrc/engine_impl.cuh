@@ -1093,6 +1093,31 @@ class Engine final : public EngineBase {
     GLIA_LAUNCH_CHECK();
   }
   void set_obs_filter(const void* f) override { import_field(f, obs_); }
+  // the observation operator at t = 0 of the two-snapshot objective (Obs::filter_0_, 1 until set)
+  R* obs0() {
+    if (!obs0_) {
+      obs0_ = fld();
+      fill(obs0_, 1.0);
+    }
+    return obs0_;
+  }
+  void set_obs_threshold0(const void* data, double thr) override {
+    import_field(data, tmp_);
+    k_threshold<R><<<pw_blocks_, kThreads, 0, stream_>>>(N_, tmp_, thr, obs0());
+    GLIA_LAUNCH_CHECK();
+  }
+  void set_obs_filter0(const void* f) override { import_field(f, obs0()); }
+  // Data::dt0 with TumorParameters::two_time_points_: J gains h^3/2 ||O0 c(0) - d0||^2 and the p
+  // gradient h^3 Phi^T O0^T (O0 c(0) - d0); NULL ends the two-snapshot objective
+  void set_data0(const void* d0) override {
+    if (!d0) {
+      two_tp_ = false;
+      return;
+    }
+    if (!d0_) d0_ = fld();
+    import_field(d0, d0_);
+    two_tp_ = true;
+  }
   void set_c0(const void* c0) override { import_field(c0, c0_); }
 
   // ------------------------------------------------------------------------------------------
@@ -1453,6 +1478,8 @@ class Engine final : public EngineBase {
                                         std::to_string(nx()) + " (np + nk + nr)");
     if (!state_done_)
       throw Error(GLIA_ERR_STATE, "evaluateHessian needs a preceding state solve or gradient");
+    if (two_tp_)  // as the reference (src/grad/DerivativeOperatorsRD.cpp:234)
+      throw Error(GLIA_ERR_INVALID, "evaluateHessian is not implemented for two snapshots");
     if (opt_.diffusivity_inversion) {
       hessian_diffusivity(x, y);
       return;
@@ -1603,6 +1630,15 @@ class Engine final : public EngineBase {
     import_field(d1, data);
     update_coefficients(x);
     if (apply_phi()) phi_apply_into(c0_, x);
+    // two snapshots: ||O0 c(0) - d0||^2 and r0 = -O0^T (O0 c(0) - d0)
+    double m0 = 0;
+    if (two_tp_) {
+      if (want_grad && !r0_) r0_ = fld();
+      GLIA_TIMED(KS_OBS, FB() * (want_grad ? 4 : 3),
+                 k_obs_residual<R><<<red_blocks_, kThreads, 0, stream_>>>(
+                     N_, c0_, obs0(), d0_, want_grad ? r0_ : nullptr, sc_, ws_));
+      m0 = read_red(0);
+    }
     solve_state_internal();
     const double h = 2.0 * M_PI / g_.n, h3 = h * h * h;
     GLIA_TIMED(KS_OBS, FB() * (want_grad ? 4 : 3),
@@ -1612,6 +1648,11 @@ class Engine final : public EngineBase {
     if (want_grad) {
       solve_adjoint_internal(true);
       if (apply_phi()) p_gradient(x, dJ, h3);
+      if (two_tp_) {  // dJ_p += h^3 Phi^T O0^T (O0 c(0) - d0) (:189-196)
+        std::vector<double> pr(std::max({opt_.np, phi_np_, 1}));
+        phi_applyT_from(r0_, pr.data());
+        for (int i = 0; i < np; i++) dJ[i] += h3 * (-pr[i]);
+      }
     }
     double reg = 0;
     if (opt_.regularization_norm == 0) {
@@ -1620,7 +1661,7 @@ class Engine final : public EngineBase {
       for (int i = 0; i < np; i++) reg += x[i] * x[i];
       reg *= 0.5 * opt_.beta;
     }
-    if (J) *J = h3 * 0.5 * m1 + reg;
+    if (J) *J = h3 * 0.5 * (m1 + m0) + reg;
     if (!want_grad) return;
     // gradDiffusion / gradReaction (src/grad/DerivativeOperators.cpp:189-321)
     double acc[8];
@@ -2060,6 +2101,9 @@ class Engine final : public EngineBase {
   // field, the reference's p_[nt] and c_[nt] of checkpointed runs
   R *ksec_ = nullptr, *inc_ = nullptr, *pnt_ = nullptr, *cfin_ = nullptr;
   bool ksec_set_ = false;
+  // two-snapshot objective: O at t = 0, d0, and -O0^T (O0 c(0) - d0)
+  R *obs0_ = nullptr, *d0_ = nullptr, *r0_ = nullptr;
+  bool two_tp_ = false;
   R *chat_ = nullptr, *xhat_ = nullptr, *rhat_ = nullptr, *phat_ = nullptr, *what_ = nullptr;
   R *g3s_ = nullptr, *g3r_ = nullptr, *ga3_ = nullptr;
   R* wkern_ = nullptr;

@@ -167,6 +167,16 @@ int glia_phi_apply_transpose(glia_ctx* ctx, const void* v, double* pout);
 int glia_set_obs_threshold(glia_ctx* ctx, const void* data, double thr);
 /* Obs::setCustomFilter (src/mat/Obs.cpp:57-69). */
 int glia_set_obs_filter(glia_ctx* ctx, const void* filter);
+/* The same two for the observation operator at t = 0 of the two-snapshot objective
+ * (Obs::setDefaultFilter / setCustomFilter with time_point 0, filter_0_; 1 until set). */
+int glia_set_obs_threshold0(glia_ctx* ctx, const void* data, double thr);
+int glia_set_obs_filter0(glia_ctx* ctx, const void* filter);
+/* Data::dt0 with TumorParameters::two_time_points_ (include/utils/Utils.h:99-124): the data at
+ * t = 0. With it the objective gains h^3/2 ||O0 c(0) - d0||^2 and the p gradient
+ * h^3 Phi^T O0^T (O0 c(0) - d0) (src/grad/DerivativeOperatorsRD.cpp:29-33, 114-120, 148-152,
+ * 189-196); the Hessian returns GLIA_ERR_INVALID as the reference's (:234). d0 = NULL goes back to
+ * one snapshot. */
+int glia_set_data0(glia_ctx* ctx, const void* d0);
 
 /* ---- PDE operators --------------------------------------------------------------------------- */
 /* Tumor::c_0_ (used by the derivative operators when flag_reaction_inv is set). */

@@ -266,6 +266,9 @@ struct Ctx {
   std::vector<double> phi_max_each;
   // Obs
   Field obs_filter;
+  // two snapshots (TumorParameters::two_time_points_): Obs::filter_0_ and Data::dt0
+  Field obs_filter0, data0;
+  bool two_tp = false;
   // Tumor state
   Field c0, ct, p0, pt;
   // PdeOperatorsRD history
@@ -910,6 +913,10 @@ struct Ctx {
       err = "evaluateHessian needs a preceding state solve or gradient";
       return GLIA_ERR_STATE;
     }
+    if (two_tp) {  // :234
+      err = "evaluateHessian is not implemented for two snapshots";
+      return GLIA_ERR_INVALID;
+    }
     if (opt.diffusivity_inversion) return hessianDiffusivity(x, y);
     const int np_ = opt.np;
     phi_apply(c0.data(), x);
@@ -1012,6 +1019,15 @@ struct Ctx {
     if (want_grad) std::fill(dJ, dJ + nx(), 0.0);
     updateReactionAndDiffusion(x);
     if (apply_phi()) phi_apply(c0.data(), x);
+    // ||O0 c(0) - d0||^2 (:148-152)
+    double m0 = 0;
+    Field r0;
+    if (two_tp) {
+      r0.assign(N, 0.0);
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < N; i++) r0[i] = c0[i] * obs_filter0[i] - data0[i];
+      m0 = vdot(r0.data(), r0.data(), N);
+    }
     int rc = solveState(0);
     if (rc) return rc;
     Field tmp(N);
@@ -1039,6 +1055,13 @@ struct Ctx {
           }
         }
       }
+      if (two_tp) {  // dJ += h^3 Phi^T O0^T (O0 c(0) - d0) (:189-196)
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < N; i++) r0[i] *= obs_filter0[i];
+        std::vector<double> pr(std::max(np_, 1));
+        phi_applyT(pr.data(), r0.data());
+        for (int i = 0; i < np_; i++) dJ[i] += h3 * pr[i];
+      }
     }
     double reg = 0;
     if (opt.regularization_norm == 0) {
@@ -1047,7 +1070,7 @@ struct Ctx {
       for (int i = 0; i < np_; i++) reg += x[i] * x[i];
       reg *= 0.5 * opt.beta;
     }
-    if (J) *J = h3 * 0.5 * m1 + reg;
+    if (J) *J = h3 * 0.5 * (m1 + m0) + reg;
     if (want_grad) {
       gradDiffusion(dJ);
       gradReaction(dJ);
@@ -1197,6 +1220,28 @@ int oracle_glia_set_obs_threshold(glia_ctx* ctx, const double* data, double thr)
 int oracle_glia_set_obs_filter(glia_ctx* ctx, const double* f) {
   if (!ctx || !f) return GLIA_ERR_INVALID;
   std::copy(f, f + ctx->N, ctx->obs_filter.begin());
+  return GLIA_OK;
+}
+int oracle_glia_set_obs_threshold0(glia_ctx* ctx, const double* data, double thr) {
+  if (!ctx || !data) return GLIA_ERR_INVALID;
+  ctx->obs_filter0.assign(ctx->N, 0.0);
+  for (int64_t i = 0; i < ctx->N; i++) ctx->obs_filter0[i] = double(data[i] > thr);
+  return GLIA_OK;
+}
+int oracle_glia_set_obs_filter0(glia_ctx* ctx, const double* f) {
+  if (!ctx || !f) return GLIA_ERR_INVALID;
+  ctx->obs_filter0.assign(f, f + ctx->N);
+  return GLIA_OK;
+}
+int oracle_glia_set_data0(glia_ctx* ctx, const double* d0) {
+  if (!ctx) return GLIA_ERR_INVALID;
+  if (!d0) {
+    ctx->two_tp = false;
+    return GLIA_OK;
+  }
+  ctx->data0.assign(d0, d0 + ctx->N);
+  if ((int64_t)ctx->obs_filter0.size() != ctx->N) ctx->obs_filter0.assign(ctx->N, 1.0);
+  ctx->two_tp = true;
   return GLIA_OK;
 }
 int oracle_glia_set_c0(glia_ctx* ctx, const double* c0) {
