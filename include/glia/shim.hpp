@@ -37,6 +37,7 @@ struct TumorParameters {
   ScalarType obs_threshold_1_ = 0;
   std::array<ScalarType, 3> user_cm_{{M_PI, M_PI, M_PI}};
   bool adjoint_store_ = false, phi_store_ = false;
+  bool two_time_points_ = false;  // objective with data at t = 0 as well (Data::dt0)
 };
 
 struct OptimizerSettings {
@@ -231,10 +232,11 @@ class PdeOperatorsRD {
   std::shared_ptr<SpectralOperators> spec_ops_;
 };
 
-// Data (include/utils/Utils.h:99-124): the observation at t = 1
+// Data (include/utils/Utils.h:99-124): the observations at t = 1 and (two snapshots) t = 0
 struct Data {
-  Vec t1;
+  Vec t1, t0;
   const Vec& dt1() const { return t1; }
+  const Vec& dt0() const { return t0; }
 };
 
 // DerivativeOperatorsRD (src/grad/DerivativeOperatorsRD.cpp)
@@ -247,12 +249,19 @@ class DerivativeOperatorsRD {
     glia_opt_settings s = to_opt(*params_, all_gradients_);
     return glia_set_opt(ctx(), &s);
   }
+  // the t = 0 data of the two-snapshot objective, or back to one snapshot
+  PetscErrorCode sync_data(const Data& data) {
+    const bool two = params_->tu_->two_time_points_ && !data.dt0().empty();
+    return glia_set_data0(ctx(), two ? data.dt0().data() : nullptr);
+  }
   PetscErrorCode evaluateObjective(ScalarType* J, const Vec& x, std::shared_ptr<Data> data) {
     int rc = sync_settings();
+    if (!rc) rc = sync_data(*data);
     return rc ? rc : glia_eval_objective(ctx(), x.data(), (int)x.size(), data->dt1().data(), J);
   }
   PetscErrorCode evaluateGradient(Vec& dJ, const Vec& x, std::shared_ptr<Data> data) {
     int rc = sync_settings();
+    if (!rc) rc = sync_data(*data);
     dJ.assign(x.size(), 0.0);
     return rc ? rc
               : glia_eval_gradient(ctx(), x.data(), (int)x.size(), data->dt1().data(), dJ.data());
@@ -260,6 +269,7 @@ class DerivativeOperatorsRD {
   PetscErrorCode evaluateObjectiveAndGradient(ScalarType* J, Vec& dJ, const Vec& x,
                                               std::shared_ptr<Data> data) {
     int rc = sync_settings();
+    if (!rc) rc = sync_data(*data);
     dJ.assign(x.size(), 0.0);
     return rc ? rc
               : glia_eval_objective_and_gradient(ctx(), x.data(), (int)x.size(),
