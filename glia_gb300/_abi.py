@@ -28,6 +28,7 @@ GLIA_PTR_DEVICE_F64 = 1
 GLIA_PTR_DEVICE_F32 = 2
 GLIA_HISTORY_FULL = 0
 GLIA_HISTORY_CHECKPOINT = 1
+GLIA_HISTORY_OFF = 2
 GLIA_PC_DT_REFERENCE = 0
 GLIA_PC_DT_FIXED = 1
 GLIA_PC_DT_MATCHED = 2

@@ -202,7 +202,7 @@ class Engine final : public EngineBase {
     pc_dt_fixed_ = pc_dt;
   }
   void set_history(int mode, int every, int adjoint_store) override {
-    if (mode != GLIA_HISTORY_FULL && mode != GLIA_HISTORY_CHECKPOINT)
+    if (mode != GLIA_HISTORY_FULL && mode != GLIA_HISTORY_CHECKPOINT && mode != GLIA_HISTORY_OFF)
       throw Error(GLIA_ERR_INVALID, "set_history: unknown mode");
     if (mode == GLIA_HISTORY_CHECKPOINT && (every < 1 || ref_))
       throw Error(GLIA_ERR_INVALID,
@@ -1142,6 +1142,10 @@ class Engine final : public EngineBase {
   }
   void ensure_history() {
     const bool store_half = !ref_ || adjoint_store_;
+    if (hist_mode_ == GLIA_HISTORY_OFF) {
+      release_history();
+      return;
+    }
     if (full()) {
       if ((int)c_hist_.size() != nt_ + 1) {
         release_history();
@@ -1203,6 +1207,13 @@ class Engine final : public EngineBase {
     st_.diff_ksp_itr_state = 0;
     vcopy(ct_, c0_);
     const bool trick = kappa_trick_ok();
+    if (hist_mode_ == GLIA_HISTORY_OFF) {  // time_history_off_: the state only
+      for (int i = 0; i < nt_; i++) step(ct_, nullptr, nullptr);
+      sync_sweep();
+      state_done_ = false;  // nothing to linearise around or sweep back over
+      adjoint_done_ = false;
+      return;
+    }
     if (full()) {
       vcopy(c_hist_[0], ct_);
       for (int i = 0; i < nt_; i++) {
@@ -1369,6 +1380,8 @@ class Engine final : public EngineBase {
   // reference it leaves p_[nt] of the full history untouched.
   // skip_final leaves out the t = 1 term of the accumulation (the Hessian adds its own).
   void solve_adjoint_internal(bool accumulate, int linearized = 1, bool skip_final = false) {
+    if (hist_mode_ == GLIA_HISTORY_OFF)
+      throw Error(GLIA_ERR_STATE, "solveAdjoint: no time history (GLIA_HISTORY_OFF)");
     if (!state_done_) throw Error(GLIA_ERR_STATE, "solveAdjoint needs a preceding solveState");
     st_.nb_adjoint_solves++;
     st_.diff_ksp_itr_adj = 0;

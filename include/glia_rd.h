@@ -58,6 +58,8 @@ extern "C" {
 /* Time history kept for the adjoint (PdeOperatorsRD ctor, src/pde/PdeOperators.cpp:17-55). */
 #define GLIA_HISTORY_FULL 0       /* every state c_[0..nt] (and c_half_ when adjoint_store) */
 #define GLIA_HISTORY_CHECKPOINT 1 /* every k-th state; segments recomputed in the adjoint    */
+#define GLIA_HISTORY_OFF 2        /* time_history_off_: no states kept (forward-only runs);  */
+                                  /* adjoint, gradient and Hessian return GLIA_ERR_STATE     */
 
 /* Which dt the spectral preconditioner is built with (DiffusionSolver::precFactor,
  * src/pde/DiffusionSolver.cpp:119-180, reads ctx_->dt_, which solve() overwrites at :226). */

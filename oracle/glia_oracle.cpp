@@ -274,6 +274,7 @@ struct Ctx {
   // PdeOperatorsRD history
   std::vector<Field> c_hist, p_hist, c_half;
   bool state_done = false;
+  bool history_off = false;  // TumorParameters::time_history_off_: no states kept
   // DiffCoef::temp_[7]: sum_i m_i k~_i of the Hessian's diffusivity direction
   Field ksec;
   // scratch
@@ -790,6 +791,27 @@ struct Ctx {
     }
     st.nb_state_solves++;
     vcopy(ct.data(), c0.data(), N);
+    if (linearized == 0 && history_off) {  // the state only (solveState(0), :252-254, 295-298)
+      c_hist.clear();
+      c_half.clear();
+      state_done = false;
+      st.diff_ksp_itr_state = 0;
+      for (int i = 0; i < nt; i++) {
+        int rc;
+        if (order == 2) {
+          if ((rc = solve(ct.data(), dt / 2.0))) return rc;
+          st.diff_ksp_itr_state += ksp_itr;
+          reaction(ct.data(), nullptr, 0);
+          if ((rc = solve(ct.data(), dt / 2.0))) return rc;
+          st.diff_ksp_itr_state += ksp_itr;
+        } else {
+          if ((rc = solve(ct.data(), dt))) return rc;
+          st.diff_ksp_itr_state += ksp_itr;
+          reaction(ct.data(), nullptr, 0);
+        }
+      }
+      return 0;
+    }
     if (linearized == 0) {
       c_hist.assign(nt + 1, Field());
       c_half.assign(adjoint_store ? nt : 0, Field());
@@ -833,6 +855,10 @@ struct Ctx {
     return 0;
   }
   int solveAdjoint(int linearized) {
+    if (history_off) {
+      err = "solveAdjoint: no time history (GLIA_HISTORY_OFF)";
+      return GLIA_ERR_STATE;
+    }
     if (!state_done) {
       err = "solveAdjoint needs a preceding solveState";
       return GLIA_ERR_STATE;
@@ -1135,10 +1161,11 @@ int oracle_glia_set_pcg(glia_ctx* ctx, double rtol, int maxit, int pc_dt_mode, d
   return GLIA_OK;
 }
 int oracle_glia_set_history(glia_ctx* ctx, int mode, int every, int adjoint_store) {
-  (void)mode;
-  (void)every;
-  if (!ctx) return GLIA_ERR_INVALID;
+  (void)every;  // the oracle keeps every state; checkpointing changes no result
+  if (!ctx || mode < GLIA_HISTORY_FULL || mode > GLIA_HISTORY_OFF) return GLIA_ERR_INVALID;
   ctx->adjoint_store = adjoint_store != 0;
+  ctx->history_off = mode == GLIA_HISTORY_OFF;
+  ctx->state_done = false;
   return GLIA_OK;
 }
 int oracle_glia_set_opt(glia_ctx* ctx, const glia_opt_settings* s) {
