@@ -38,6 +38,7 @@ struct TumorParameters {
   std::array<ScalarType, 3> user_cm_{{M_PI, M_PI, M_PI}};
   bool adjoint_store_ = false, phi_store_ = false;
   bool two_time_points_ = false;  // objective with data at t = 0 as well (Data::dt0)
+  bool time_history_off_ = false; // forward-only runs: no states kept
 };
 
 struct OptimizerSettings {
@@ -206,8 +207,8 @@ class PdeOperatorsRD {
       : tumor_(t), params_(p), spec_ops_(s) {
     auto& tu = *p->tu_;
     glia_set_time(s->ctx_, tu.dt_, tu.nt_, tu.order_);
-    glia_set_history(s->ctx_, p->engine_.history, p->engine_.checkpoint_every,
-                     tu.adjoint_store_);
+    glia_set_history(s->ctx_, tu.time_history_off_ ? GLIA_HISTORY_OFF : p->engine_.history,
+                     p->engine_.checkpoint_every, tu.adjoint_store_);
   }
   PetscErrorCode solveState(int linearized) {
     int rc = glia_solve_state(spec_ops_->ctx_, linearized, tumor_->c_0_.data(),
