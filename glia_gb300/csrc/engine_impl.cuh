@@ -2072,7 +2072,7 @@ class Engine final : public EngineBase {
   cufftHandle r2c2d3_ = 0, c2r2d3_ = 0;  // batched 2-D (y, z) transforms, 3n planes
   float2* tw256_ = nullptr;
   int xres_inv_ = 0, xres_fwd_ = 0;  // resident CTAs of k_xinv / k_xfwd on this device
-  int own_res_[3] = {0, 0, 0};       // ... of k_yinv, k_zpass, k_yfwd
+  int own_res_[3] = {0, 0, 0};       // ... of the y-inverse pass, the z pass, k_yfwd
   CUtensorMap kmap_{};               // TMA map of the packed line arrays (k_yfwd)
   bool tma_ = false;                 // k_yfwd stages with TMA copies (GLIA_TMA=1)
   bool zpass2_ = true;               // z pass with two real lines per complex transform

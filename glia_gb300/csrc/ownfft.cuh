@@ -3,12 +3,16 @@
 //
 //   k_xinv<OUT2>  p (or P r + b p) -> G_x = F_x^-1(i w_x p) / N, G_0 = F_x^-1(p) / N
 //                 layout (x, ky, kz) with kz < n/2 + 1, the cuFFT half-spectrum order
-//   k_yinv        G -> H_x = F_y^-1 G_x, H_y = F_y^-1(i w_y G_0), H_0 = F_y^-1 G_0
+//   k_yinv_bulk / k_yinv
+//                 G -> H_x = F_y^-1 G_x, H_y = F_y^-1(i w_y G_0), H_0 = F_y^-1 G_0
 //                 layout (x, y, kz'), kz' < n/2: the kz = 0 and kz = n/2 columns travel packed
-//                 as one complex column G(kz = 0) + i G(kz = n/2)
-//   k_zpass       per (x, y) line: packed half spectrum -> real line (C2R through an n/2-point
-//                 complex transform), times k, back (R2C), packed; H_0 gets i w_z on both sides
-//                 -> K_x, K_y, L_z = i w_z F_z(k d_z p), in place
+//                 as one complex column G(kz = 0) + i G(kz = n/2); input rows staged by bulk
+//                 copies (k_yinv_bulk, default) or cp.async (k_yinv)
+//   k_zpass2 / k_zpass
+//                 per (x, y) line: packed half spectrum -> real line, times k, back, packed;
+//                 H_0 gets i w_z on both sides -> K_x, K_y, L_z = i w_z F_z(k d_z p), in place.
+//                 k_zpass2 (default, zpass2.cuh): two real lines per complex transform;
+//                 k_zpass (here): C2R / R2C through an n/2-point complex transform
 //   k_yfwd        K -> M_x = F_y K_x, M_r = i w_y F_y K_y + F_y L_z, unpacked into the kz = 0
 //                 and kz = n/2 columns, layout (x, ky, kz) with kz < n/2 + 1
 //   k_xfwd<IN2>   divergence i w_x F_x M_x + F_x M_r and the PCG epilogue.
