@@ -2,9 +2,10 @@
 // forward / adjoint / gradient path.
 //
 // This file restates, in plain C++17 + OpenMP and double precision, the algorithm of the
-// reference (ShashankSubramanian/GLIA). It is the reference the CUDA library is tested against and the timed
-// CPU baseline; the product never links, loads or calls it. Only tests/, __graft_entry__.smoke() and
-// bench.py's CPU legs use it.
+// reference (ShashankSubramanian/GLIA): the state and adjoint solves (including the linearised
+// ones of the Hessian), the objective (one or two snapshots), the gradient, both Hessian branches.
+// It is what the CUDA library is tested against, and the timed CPU baseline; the product never
+// links, loads or calls it. Only tests/, __graft_entry__.smoke() and bench.py's CPU legs use it.
 //
 // Pins (see tests/test_oracle_pins.py):
 //  - src/test/pdesolver.cpp:46-48 known answer: 64^3, sinusoidal k (scale 1e-2), Gaussian test
