@@ -13,7 +13,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def header_functions():
-    txt = open(os.path.join(ROOT, "include", "glia_rd.h")).read()
+    with open(os.path.join(ROOT, "include", "glia_rd.h")) as f:
+        txt = f.read()
     return sorted(set(re.findall(r"\b(glia_[a-z0-9_]+)\s*\(", txt)))
 
 

@@ -28,7 +28,7 @@ def test_objective_backward_is_the_adjoint_gradient():
     J = ga.rd_objective(x, ctx, d1)
     J.backward()
     J_ref, g_ref = ctx.eval_objective_and_gradient(x.detach().numpy(), d1)
-    assert float(J) == pytest.approx(J_ref, rel=1e-14)
+    assert J.item() == pytest.approx(J_ref, rel=1e-14)
     assert np.allclose(x.grad.numpy(), g_ref, rtol=1e-13, atol=0)
 
 

@@ -46,7 +46,7 @@ def _rank(rank, ws, port, out):
 
 def test_two_gloo_ranks_weak_scaling():
     ws, port = 2, _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork of this threaded process
         out = m.dict()
         mp.spawn(_rank, args=(ws, port, out), nprocs=ws, join=True)
         res = dict(out)
@@ -116,7 +116,7 @@ def test_lpt_partition():
 
 def test_two_gloo_ranks_sharded_batch():
     ws, port = 2, _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork of this threaded process
         out = m.dict()
         mp.spawn(_batch_rank, args=(ws, port, out), nprocs=ws, join=True)
         res = dict(out)
