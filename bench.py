@@ -386,7 +386,8 @@ def run_ours(args, torch, api, wl, tissue, centers, stream, ws, rank):
            "J": J}
 
     # ---- FP64 GPU legs: our fused FP64 and the reference-structured plain FP64 path ---------
-    if not args.no_fp64 and rank == 0:
+    # (one-GPU runs only: under torchrun they would hold every rank's GPU for minutes)
+    if not args.no_fp64 and rank == 0 and ws == 1:
         legs = {}
         ref_grad = None
         for name, prec, engine, every in (("fp64_fused", _abi.GLIA_FP64, _abi.GLIA_ENGINE_FUSED, args.every),
