@@ -70,3 +70,19 @@ def test_phi_mesh_matches_reference_lattice():
         b = phi_mesh(orc_api, np_, [np.pi, np.pi, np.pi], 2 * np.pi / 64, 1.5)
         assert np.array_equal(a, b)
         assert len(np.unique(a.round(12), axis=0)) == np_
+
+
+def test_header_is_plain_c99():
+    """The boundary header must compile as C (no C++ types cross the ABI)."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+
+        pytest.skip("no C compiler")
+    r = subprocess.run([cc, "-x", "c", "-std=c99", "-fsyntax-only", "-Wall", "-Wextra",
+                        "-pedantic", "-Werror", os.path.join(ROOT, "include", "glia_rd.h")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
