@@ -86,3 +86,24 @@ def test_header_is_plain_c99():
                         "-pedantic", "-Werror", os.path.join(ROOT, "include", "glia_rd.h")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_cpp_shim_header_compiles():
+    """include/glia/shim.hpp (the reference's class names over the C-ABI) compiles as C++17."""
+    import shutil
+    import subprocess
+    import tempfile
+
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        import pytest
+
+        pytest.skip("no C++ compiler")
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "use_shim.cpp")
+        with open(src, "w") as f:
+            f.write('#include "glia/shim.hpp"\nint main() { return 0; }\n')
+        r = subprocess.run([cxx, "-std=c++17", "-fsyntax-only", "-Wall", "-Wextra", "-Werror",
+                            "-I", os.path.join(ROOT, "include"), src],
+                           capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
