@@ -209,19 +209,20 @@ def test_gpu_hessian_checkpointed_equals_full_history():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision,engine,history,tol", [
-    (_abi.GLIA_FP64, _abi.GLIA_ENGINE_FUSED, _abi.GLIA_HISTORY_FULL, 1e-9),
-    (_abi.GLIA_FP64, _abi.GLIA_ENGINE_FUSED, _abi.GLIA_HISTORY_CHECKPOINT, 1e-9),
-    (_abi.GLIA_FP64, _abi.GLIA_ENGINE_REFERENCE, _abi.GLIA_HISTORY_FULL, 1e-9),
-    (_abi.GLIA_MIXED, _abi.GLIA_ENGINE_FUSED, _abi.GLIA_HISTORY_FULL, 1e-4),
-    (_abi.GLIA_MIXED, _abi.GLIA_ENGINE_FUSED, _abi.GLIA_HISTORY_CHECKPOINT, 1e-4),
+@pytest.mark.parametrize("precision,engine,history,tol,n", [
+    (_abi.GLIA_FP64, _abi.GLIA_ENGINE_FUSED, _abi.GLIA_HISTORY_FULL, 1e-9, 32),
+    (_abi.GLIA_FP64, _abi.GLIA_ENGINE_FUSED, _abi.GLIA_HISTORY_CHECKPOINT, 1e-9, 32),
+    (_abi.GLIA_FP64, _abi.GLIA_ENGINE_REFERENCE, _abi.GLIA_HISTORY_FULL, 1e-9, 32),
+    (_abi.GLIA_MIXED, _abi.GLIA_ENGINE_FUSED, _abi.GLIA_HISTORY_FULL, 1e-4, 32),
+    (_abi.GLIA_MIXED, _abi.GLIA_ENGINE_FUSED, _abi.GLIA_HISTORY_CHECKPOINT, 1e-4, 32),
+    # 64^3 FP32: the own x / y / z transform kernels, whose z pass reads k~ for the D~ apply
+    (_abi.GLIA_MIXED, _abi.GLIA_ENGINE_FUSED, _abi.GLIA_HISTORY_CHECKPOINT, 1e-4, 64),
 ])
-def test_gpu_diffusivity_hessian_matches_oracle(precision, engine, history, tol):
+def test_gpu_diffusivity_hessian_matches_oracle(precision, engine, history, tol, n):
     """Hessian with diffusivity inversion (p and kappa blocks, the t = 1 term from p_[nt]) and
     solveState(2) against the oracle, at a nonzero residual so that p_[nt] is not 0."""
     from tests.gpu_common import gpu
 
-    n = 32
     octx, wl, x, rng = _problem(_orc, n, nt=6, diffusivity=1)
     gctx, _, _, _ = _problem(lambda m: gpu(m, precision, engine), n, nt=6, history=history,
                              every=4, diffusivity=1)
