@@ -154,93 +154,117 @@ def build_workload(args, seed_offset=0):
     return wl, tissue, centers
 
 
-def cpu_sample(wl, tissue, c0_host, threads=None):
-    """One Crank–Nicolson diffusion solve (dt/2) and one D apply of the FP64 CPU oracle at the
-    workload's grid, on the state c0; returns (seconds per solve, seconds per D apply, its)."""
-    from oracle import oracle
+def fixture_data(wl):
+    """The thresholded observation of the FP64 oracle's stored evaluation of this workload
+    (tests/golden/workload256*), or None when the workload is not the stored one."""
+    try:
+        from tests.golden.make_config1 import load, load_data
+        want = load(wl.n)
+    except (OSError, ImportError):
+        return None, None
+    if (want["nt"], want["n_gauss"], want["rho"], want["kappa"]) != (wl.nt, wl.n_gauss, wl.rho,
+                                                                     wl.kappa):
+        return None, None
+    return load_data(wl.n), want
 
-    if threads:
+
+class OracleSample:
+    """The FP64 CPU oracle (the port of the reference's CPU path: CN-PCG with the spectral
+    preconditioner, Strang splitting, full time history with recomputed half steps, Phi, adjoint,
+    trapezoid kappa/rho gradients) set up for the workload with nt_sample time steps. One sample
+    is one complete glia_eval_objective_and_gradient call (forward, adjoint, gradient, Phi and
+    Phi^T) at the workload's grid; a gradient evaluation at nt steps costs about nt / nt_sample
+    samples (the per-evaluation Phi work is counted nt / nt_sample times, so the extrapolation
+    slightly overstates the CPU time per evaluation)."""
+
+    def __init__(self, wl, tissue, centers, d, threads, nt_sample=1):
+        from glia_gb300 import _abi
+        from glia_gb300 import synthetic as syn
+        from oracle import oracle
+
         oracle.set_num_threads(threads)
+        self.wl, self.nt_sample, self.threads = wl, nt_sample, threads
+        self.o = oracle.context(wl.n)
+        syn.setup_context(self.o, wl, tissue, centers, _abi.GLIA_HISTORY_FULL, 0)
+        self.o.set_time(wl.dt, nt_sample, 2)
+        self.o.set_obs_filter(np.ones(wl.n ** 3))
+        self.d = d
+        self.x = wl.x_eval()
+
+    def step(self):
+        """Seconds of one sample."""
+        t0 = time.perf_counter()
+        self.o.eval_objective_and_gradient(self.x, self.d)
+        return time.perf_counter() - t0
+
+    def evals_per_s(self, t_step):
+        return self.nt_sample / (t_step * self.wl.nt)
+
+    def describe(self, t_step, fixture):
+        st = self.o.stats()
+        its = st["total_pcg_iterations"] / max(1, st["total_diffusion_solves"])
+        return (f"one full FP64 oracle gradient evaluation (forward, adjoint with recomputed half "
+                f"steps, kappa/rho/p gradients) of the {self.wl.n}^3 workload with nt = "
+                f"{self.nt_sample} on {self.threads} threads, {t_step:.2f} s ({its:.1f} PCG its "
+                f"per solve, data {'of the oracle fixture' if fixture else 'stand-in'}); "
+                f"extrapolated to nt = {self.wl.nt} as {self.wl.nt // self.nt_sample} such "
+                f"evaluations")
+
+
+def reference_data(wl, tissue, centers):
+    d, want = fixture_data(wl)
+    if d is not None:
+        return d, True
+    # stand-in data for other sizes: the thresholded initial condition of the perturbed p
+    from oracle import oracle
+    from glia_gb300 import _abi
+    from glia_gb300 import synthetic as syn
+
     o = oracle.context(wl.n)
-    o.set_time(wl.dt, wl.nt, 2)
-    o.set_tissue(*tissue.flat())
-    o.set_coefficients(k=wl.kappa, rho=wl.rho, k_gm_wm=wl.k_gm_wm)
-    c = np.array(c0_host, dtype=np.float64)
-    t0 = time.perf_counter()
-    its = o.diffusion_solve(c, wl.dt / 2)
-    t_solve = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    o.apply_d(c)
-    t_d = time.perf_counter() - t0
-    return t_solve, t_d, its
-
-
-def cpu_eval_seconds(wl, t_solve, t_d):
-    """The reference's gradient evaluation at its defaults: 2nt state solves, 2nt adjoint solves
-    plus nt recomputed half steps (adjoint_store_ = false), and the trapezoid kappa gradient with
-    8 transforms per time point (0.8 of a D apply's 10)."""
-    return 5 * wl.nt * t_solve + 0.8 * (wl.nt + 1) * t_d
-
-
-def approx_state(wl, tissue, centers):
-    """Stand-in initial state on the host: the active Gaussians of p, filtered by the brain."""
-    n = wl.n
-    h = 2 * np.pi / n
-    X = np.arange(n) * h
-    p = wl.p_true()
-    c = np.zeros((n, n, n))
-    filt = ((tissue.wm > 0.1) | (tissue.gm > 0.1)).astype(np.float64)
-    for i in np.nonzero(p)[0]:
-        cx, cy, cz = centers[i]
-        r2 = (X[:, None, None] - cx) ** 2 + (X[None, :, None] - cy) ** 2 + (X[None, None, :] - cz) ** 2
-        c += p[i] * np.exp(-r2 / (2 * wl.sigma ** 2))
-    return (c * filt).reshape(-1)
+    syn.setup_context(o, wl, tissue, centers, _abi.GLIA_HISTORY_FULL, 0)
+    c = o.phi_apply(wl.p_obs())
+    return (c > 0.5 * c.max()).astype(np.float64), False
 
 
 # ------------------------------------------------------------------------------------------
 def run_reference(args):
-    """The reference's CPU implementation of the path (the FP64 oracle port of it) on the host
-    cores; each step is one diffusion solve + one D apply of the 256^3 workload, extrapolated to
-    gradient evaluations per second."""
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    """The reference's CPU implementation of the path (the FP64 oracle port of it) on all host
+    cores. Each step is one complete gradient evaluation of the workload at nt = 1 (every stage
+    of the path at full grid size); `value` extrapolates it to nt = args.nt."""
     rank = int(os.environ.get("RANK", "0"))
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
-    from oracle import oracle
-
     cores = os.cpu_count() or 1
-    oracle.set_num_threads(cores)
     wl, tissue, centers = build_workload(args)
-    c0 = approx_state(wl, tissue, centers)
+    d, fixture = reference_data(wl, tissue, centers)
+    smp = OracleSample(wl, tissue, centers, d, cores)
     times = []
-    its = []
     for k in range(args.warmup + args.steps):
-        t_s, t_d, it = cpu_sample(wl, tissue, c0)
+        t = smp.step()
         if k >= args.warmup:
-            times.append(cpu_eval_seconds(wl, t_s, t_d))
-            its.append(it)
-    t_eval = statistics.mean(times)
-    v = 1.0 / t_eval
-    sample = (f"per step: one CN diffusion solve (dt/2, {its[0]} PCG its) + one D apply of the "
-              f"{wl.n}^3 workload on {cores} threads, extrapolated to one gradient evaluation = "
-              f"{5 * wl.nt} solves + {0.8 * (wl.nt + 1):.1f} D applies")
+            times.append(t)
+    t_step = statistics.mean(times)
+    v = smp.evals_per_s(t_step)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_eval * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": workload_config(args, "reference CPU (oracle port)"),
+            "data": "synthetic", "config": workload_config(args),
+            "arm": "reference CPU path (FP64 oracle port), all host cores",
+            "extrapolated": {"nt_per_step": smp.nt_sample, "nt_per_evaluation": wl.nt,
+                             "seconds_per_evaluation": t_step * wl.nt / smp.nt_sample},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": sample},
+                             "sample": smp.describe(t_step, fixture)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def workload_config(args, arm):
+def workload_config(args):
     return {"workload": (f"{args.n}^3 forward+adjoint gradient of J w.r.t. (p[{args.n_gauss}], "
                          f"kappa, rho), nt={args.nt}, dt=0.01, Strang + CN-PCG (rtol 1e-6)"),
-            "arm": arm, "n": args.n, "nt": args.nt, "n_gauss": args.n_gauss,
-            "history": f"checkpoint every {args.every}" if args.every else "full",
-            "precision": "fp32 fields/transforms, fp64 reductions and scalars",
-            "l2": "flushed between timed steps (256 MiB write); per-step working set > 1 GB"}
+            "n": args.n, "nt": args.nt, "n_gauss": args.n_gauss,
+            "l2": ("per-step working set > 1 GB (larger than L2 / last-level cache); the GPU arm "
+                   "also flushes L2 (256 MiB write) between timed steps")}
 
 
 # ------------------------------------------------------------------------------------------
@@ -273,21 +297,23 @@ def run_ours(args, torch, api, wl, tissue, centers, stream, ws, rank):
 
     def make_ctx(prec, engine=_abi.GLIA_ENGINE_FUSED, every=args.every):
         ctx = Context(api, wl.n, prec, engine)
-        ctx._call("set_stream", api.set_stream, ctypes_ptr(stream.cuda_stream))
+        ctx.set_stream(stream.cuda_stream)
         hist = _abi.GLIA_HISTORY_CHECKPOINT if every else _abi.GLIA_HISTORY_FULL
         syn.setup_context(ctx, wl, tissue, centers, hist, every or 0)
         ctx.set_obs_filter(np.ones(wl.n ** 3))
         return ctx
 
     ctx = make_ctx(_abi.GLIA_MIXED)
-    # observation: forward with perturbed parameters, thresholded at 0.5
-    ctx.set_coefficients(k=wl.kappa * 0.8, rho=wl.rho * 1.2, k_gm_wm=wl.k_gm_wm)
-    c_obs0 = ctx.phi_apply(wl.p_obs())
-    c_obs1 = ctx.solve_state(c_obs0)
-    d_host = (c_obs1 > 0.5).astype(np.float64)
-    ctx.set_coefficients(k=wl.kappa, rho=wl.rho, k_gm_wm=wl.k_gm_wm)
+    # observation: forward with perturbed parameters, thresholded at 0.5 — the FP64 oracle's
+    # (stored with its full evaluation of this workload) when this is the stored workload, else
+    # this path's own forward
+    d_host, oracle_eval = fixture_data(wl) if rank == 0 else (None, None)
+    if d_host is None:
+        ctx.set_coefficients(k=wl.kappa * 0.8, rho=wl.rho * 1.2, k_gm_wm=wl.k_gm_wm)
+        c_obs1 = ctx.solve_state(ctx.phi_apply(wl.p_obs()))
+        d_host = (c_obs1 > 0.5).astype(np.float64)
+        ctx.set_coefficients(k=wl.kappa, rho=wl.rho, k_gm_wm=wl.k_gm_wm)
     x = wl.x_eval()
-    c0_host = ctx.phi_apply(wl.p_true())
 
     # ---- device-resident timed region ------------------------------------------------------
     ctx.set_pointer_mode(_abi.GLIA_PTR_DEVICE_F32)
@@ -375,7 +401,11 @@ def run_ours(args, torch, api, wl, tissue, centers, stream, ws, rank):
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32 (f64 reductions)", "data": "synthetic",
-           "config": workload_config(args, "mixed fused checkpointed GPU path"),
+           "config": workload_config(args),
+           "arm": (f"mixed fused GPU path, checkpoint every {args.every}" if args.every
+                   else "mixed fused GPU path, full history"),
+           "data_source": ("the FP64 oracle's observation (tests/golden/workload256_data.npz)"
+                           if oracle_eval else "this path's own perturbed forward"),
            "e2e": e2e, "gpu_launches": our_launches, "roofline": roofline,
            "path_gbs_algorithmic": round(path_gbs, 1) if path_gbs else None,
            "kernels": breakdown, "clocks": clk,
@@ -384,6 +414,10 @@ def run_ours(args, torch, api, wl, tissue, centers, stream, ws, rank):
                    "pcg_loop": "CUDA graph, device-side WHILE node",
                    "ffts_per_eval": st["total_fft_execs"] / args.steps},
            "J": J}
+
+    if oracle_eval is not None:
+        out.update(grad_errors(grad, np.array(oracle_eval["dJ"]), wl.n_gauss, "oracle"))
+        out["J_rel_err_vs_oracle"] = abs(J - oracle_eval["J"]) / abs(oracle_eval["J"])
 
     # ---- FP64 GPU legs: our fused FP64 and the reference-structured plain FP64 path ---------
     # (one-GPU runs only: under torchrun they would hold every rank's GPU for minutes)
@@ -418,13 +452,10 @@ def run_ours(args, torch, api, wl, tissue, centers, stream, ws, rank):
                 torch.cuda.empty_cache()
         if ref_grad is not None:
             npp = wl.n_gauss
-            out["grad_rel_err_vs_fp64"] = float(np.linalg.norm(grad - ref_grad) /
-                                                np.linalg.norm(ref_grad))
-            out["grad_rel_err_blocks"] = {
-                "p": float(np.linalg.norm(grad[:npp] - ref_grad[:npp]) /
-                           np.linalg.norm(ref_grad[:npp])),
-                "kappa": float(abs(grad[npp] - ref_grad[npp]) / abs(ref_grad[npp])),
-                "rho": float(abs(grad[npp + 1] - ref_grad[npp + 1]) / abs(ref_grad[npp + 1]))}
+            out.update(grad_errors(grad, ref_grad, npp, "fp64"))
+            if oracle_eval is not None:
+                e = grad_errors(ref_grad, np.array(oracle_eval["dJ"]), npp, "oracle")
+                legs["fp64_fused"]["grad_rel_err_vs_oracle"] = e["grad_rel_err_vs_oracle"]
             out["grad_fp64"] = {"kappa": float(ref_grad[npp]), "rho": float(ref_grad[npp + 1]),
                                 "p_norm": float(np.linalg.norm(ref_grad[:npp]))}
         out["fp64_gpu"] = legs
@@ -436,13 +467,12 @@ def run_ours(args, torch, api, wl, tissue, centers, stream, ws, rank):
     if not args.no_cpu and rank == 0 and ws == 1:
         try:
             cores = os.cpu_count() or 1
-            t_s, t_d, its = cpu_sample(wl, tissue, c0_host, threads=cores)
-            t_eval = cpu_eval_seconds(wl, t_s, t_d)
-            out["cpu_baseline"] = {
-                "value": 1.0 / t_eval, "unit": UNIT, "cores": cores, "kind": "port",
-                "sample": (f"one CN diffusion solve (dt/2, {its} PCG its, {t_s:.2f} s) + one D "
-                           f"apply ({t_d:.2f} s) of the FP64 oracle at {wl.n}^3, extrapolated to "
-                           f"{5 * wl.nt} solves + {0.8 * (wl.nt + 1):.1f} D applies per evaluation")}
+            smp = OracleSample(wl, tissue, centers, d_host, cores)
+            smp.step()  # first touch of the oracle's buffers
+            t_step = smp.step()
+            out["cpu_baseline"] = {"value": smp.evals_per_s(t_step), "unit": UNIT, "cores": cores,
+                                   "kind": "port",
+                                   "sample": smp.describe(t_step, oracle_eval is not None)}
         except Exception as exc:  # noqa: BLE001
             out["cpu_baseline"] = {"error": str(exc)[:200]}
     if rank == 0:
@@ -450,10 +480,13 @@ def run_ours(args, torch, api, wl, tissue, centers, stream, ws, rank):
     ctx.close()
 
 
-def ctypes_ptr(v):
-    import ctypes
-
-    return ctypes.c_void_p(int(v))
+def grad_errors(grad, ref, npp, name):
+    """Relative L2 error of a gradient (p[npp], kappa, rho) against `ref`, whole and per block."""
+    return {f"grad_rel_err_vs_{name}": float(np.linalg.norm(grad - ref) / np.linalg.norm(ref)),
+            f"grad_rel_err_blocks_vs_{name}": {
+                "p": float(np.linalg.norm(grad[:npp] - ref[:npp]) / np.linalg.norm(ref[:npp])),
+                "kappa": float(abs(grad[npp] - ref[npp]) / abs(ref[npp])),
+                "rho": float(abs(grad[npp + 1] - ref[npp + 1]) / abs(ref[npp + 1]))}}
 
 
 def traffic_for(kernel: str, algorithmic_per_launch: float, n: int):

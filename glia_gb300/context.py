@@ -37,6 +37,11 @@ class Context:
         rc = api.create(self.n, precision, engine, ctypes.byref(self._h))
         if rc != _abi.GLIA_OK:
             raise GliaError(rc, "create", f"n={n} precision={precision} engine={engine}")
+        # advanced by every call that rewrites the state history, the coefficients or the model
+        # settings (autograd backward passes compare it with the value seen by their forward)
+        self.generation = 0
+        self.phi_generation = 0  # advanced when the Gaussian basis may change
+        self.stream = 0          # the CUDA stream handle last given to set_stream (0 = own)
         self._opt = _abi.GliaOptSettings(np=1, nk=1, nr=1, flag_reaction_inv=0,
                                          diffusivity_inversion=1, regularization_norm=0,
                                          beta=1e-4, k_scale=1.0, rho_scale=1.0, phi_store=0,
@@ -93,6 +98,11 @@ class Context:
             out = np.empty(self.N, dtype=np.float64)
         return out, self._field_in(out)
 
+    def _touch(self, phi=False):
+        self.generation += 1
+        if phi:
+            self.phi_generation += 1
+
     def _call(self, where, fn, *args):
         self._keep = []
         try:
@@ -106,15 +116,19 @@ class Context:
         self.ptr_mode = mode
 
     def set_time(self, dt: float, nt: int, order: int = 2):
+        self._touch()
         self._call("set_time", self.api.set_time, dt, nt, order)
 
     def set_pcg(self, rtol=1e-6, maxit=5000, pc_dt_mode=_abi.GLIA_PC_DT_REFERENCE, pc_dt=0.0):
+        self._touch()
         self._call("set_pcg", self.api.set_pcg, rtol, maxit, pc_dt_mode, pc_dt)
 
     def set_history(self, mode=_abi.GLIA_HISTORY_FULL, every=0, adjoint_store=False):
+        self._touch()
         self._call("set_history", self.api.set_history, mode, every, int(adjoint_store))
 
     def set_opt(self, **kw):
+        self._touch(phi=True)
         for k, v in kw.items():
             if not hasattr(self._opt, k):
                 raise KeyError(k)
@@ -126,6 +140,7 @@ class Context:
         return self._opt.np + self._opt.nk + self._opt.nr
 
     def set_tissue(self, wm=None, gm=None, csf=None, vt=None):
+        self._touch(phi=True)
         self._keep = []
         args = [self._field_in(a) for a in (wm, gm, csf, vt)]
         try:
@@ -134,19 +149,24 @@ class Context:
             self._keep = []
 
     def set_tissue_sinusoidal(self):
+        self._touch(phi=True)
         self._call("set_tissue_sinusoidal", self.api.set_tissue_sinusoidal)
 
     def set_coefficients(self, k, rho, k_gm_wm=0.0, k_glm_wm=0.0, r_gm_wm=0.0, r_glm_wm=0.0):
+        self._touch()
         self._call("set_coefficients", self.api.set_coefficients, k, k_gm_wm, k_glm_wm, rho,
                    r_gm_wm, r_glm_wm)
 
     def set_diffusivity_sinusoidal(self, scale):
+        self._touch()
         self._call("set_diffusivity_sinusoidal", self.api.set_diffusivity_sinusoidal, scale)
 
     def prec_factor(self):
+        self._touch()
         self._call("prec_factor", self.api.prec_factor)
 
     def set_phi(self, centers, sigma, smoothing_factor=1.0):
+        self._touch(phi=True)
         c = np.ascontiguousarray(centers, dtype=np.float64).reshape(-1)
         self._call("set_phi", self.api.set_phi, _dptr(c), c.size // 3, sigma, smoothing_factor)
 
@@ -191,6 +211,7 @@ class Context:
             self._keep = []
 
     def set_c0(self, c0):
+        self._touch()
         self._keep = []
         try:
             self._check(self.api.set_c0(self._h, self._field_in(c0)), "set_c0")
@@ -200,6 +221,7 @@ class Context:
     # -- operators ------------------------------------------------------------------------
     def diffusion_solve(self, c, dt):
         """In place on `c`; returns the PCG iteration count."""
+        self._touch()
         self._keep = []
         its = ctypes.c_int(0)
         try:
@@ -253,9 +275,11 @@ class Context:
 
     def set_secondary_coefficients(self, k1, k2=0.0, k3=0.0):
         """DiffCoef::setSecondaryCoefficients: the diffusivity direction of solve_state(2)."""
+        self._touch()
         self._call("set_secondary_coefficients", self.api.set_secondary_coefficients, k1, k2, k3)
 
     def solve_state(self, c0=None, out=None, linearized=0):
+        self._touch()
         self._keep = []
         try:
             out, po = self._field_out(out)
@@ -291,6 +315,7 @@ class Context:
         return out
 
     def eval_objective(self, x, d1) -> float:
+        self._touch()
         x = np.ascontiguousarray(x, dtype=np.float64)
         J = ctypes.c_double(0)
         self._keep = []
@@ -302,6 +327,7 @@ class Context:
         return J.value
 
     def eval_gradient(self, x, d1) -> np.ndarray:
+        self._touch()
         x = np.ascontiguousarray(x, dtype=np.float64)
         dJ = np.zeros_like(x)
         self._keep = []
@@ -313,6 +339,7 @@ class Context:
         return dJ
 
     def eval_objective_and_gradient(self, x, d1):
+        self._touch()
         x = np.ascontiguousarray(x, dtype=np.float64)
         dJ = np.zeros_like(x)
         J = ctypes.c_double(0)
@@ -328,6 +355,7 @@ class Context:
     def hessian_matvec(self, x):
         """Gauss-Newton matvec y = H x of the p block (DerivativeOperatorsRD::evaluateHessian),
         linearised at the last gradient evaluation or state solve."""
+        self._touch()
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.zeros_like(x)
         self._check(self.api.hessian_matvec(self._h, _dptr(x), x.size, _dptr(y)), "hessian_matvec")
@@ -347,6 +375,7 @@ class Context:
 
     def set_stream(self, stream_handle: int):
         self._call("set_stream", self.api.set_stream, ctypes.c_void_p(int(stream_handle)))
+        self.stream = int(stream_handle)
 
     def set_timing(self, enable: bool):
         self._call("set_timing", self.api.set_timing, int(enable))

@@ -432,9 +432,14 @@ class Engine final : public EngineBase {
   template <int NN, int EPI, bool IN2>
   void xfwd_n(const R* G, const R* aux_in, const R* cx, R* out, R* aux_out, R scale, int blocks) {
     if constexpr (std::is_same<R, float>::value) {
-      if constexpr (IN2)
-        k_xfwd_own<NN, EPI><<<blocks, 256, xfwd_own_smem_bytes<NN>(), stream_>>>(
-            g_, G, aux_in, cx, out, aux_out, scale, sc_, ws_, tw256_);
+      if constexpr (IN2) {
+        if (xfwd_direct_ && EPI != EPI_APPLYD)
+          k_xfwd_own<NN, EPI, true><<<blocks, 256, xfwd_own_smem_bytes<NN>(), stream_>>>(
+              g_, G, aux_in, cx, out, aux_out, scale, sc_, ws_, tw256_);
+        else
+          k_xfwd_own<NN, EPI><<<blocks, 256, xfwd_own_smem_bytes<NN>(), stream_>>>(
+              g_, G, aux_in, cx, out, aux_out, scale, sc_, ws_, tw256_);
+      }
       else
         k_xfwd<NN, EPI><<<blocks, 256, 0, stream_>>>(g_, G, aux_in, cx, out, aux_out, scale, sc_,
                                                      ws_, tw256_);
@@ -501,9 +506,15 @@ class Engine final : public EngineBase {
         xres_inv_ = sms_ * std::min(per_sm(k_xinv<NN, 0, true>, xinv_smem_bytes<NN, 0>()),
                                     per_sm(k_xinv<NN, 1, true>, xinv_smem_bytes<NN, 1>()));
         constexpr int fs = xfwd_own_smem_bytes<NN>();
+        // forward x pass: epilogue spectra staged through the slots, or read directly by the
+        // epilogue (GLIA_XFWD_DIRECT=1)
+        const char* xd = std::getenv("GLIA_XFWD_DIRECT");
+        xfwd_direct_ = xd && xd[0] == '1';
         xres_fwd_ = sms_ * std::min({per_sm(k_xfwd_own<NN, EPI_APPLYD>, fs),
                                      per_sm(k_xfwd_own<NN, EPI_SETUP>, fs),
-                                     per_sm(k_xfwd_own<NN, EPI_CGW>, fs)});
+                                     per_sm(k_xfwd_own<NN, EPI_CGW>, fs),
+                                     per_sm(k_xfwd_own<NN, EPI_SETUP, true>, fs),
+                                     per_sm(k_xfwd_own<NN, EPI_CGW, true>, fs)});
         // y-inverse rows staged by bulk copies (default) or per-thread cp.async
         // (GLIA_YINV_BULK=0)
         const char* yb = std::getenv("GLIA_YINV_BULK");
@@ -2078,6 +2089,7 @@ class Engine final : public EngineBase {
   bool zpass2_ = true;               // z pass with two real lines per complex transform
   bool yinv_bulk_ = true;            // y-inverse rows staged by bulk copies
   bool own_ = false;  // own y and z passes (x pass on): no cuFFT inside the D apply
+  bool xfwd_direct_ = false;  // k_xfwd_own epilogue reads its spectra from global memory
   float2* tw_ = nullptr;
   char* fft_ws_ = nullptr;
   char* batch_ws_ = nullptr;

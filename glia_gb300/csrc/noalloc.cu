@@ -11,7 +11,10 @@
 // handles at most kMaxTiles * kTile voxels (2^29); larger inputs are rejected. Every call on a
 // device shares the same array and leaves its last contents behind; the counter is cleared at
 // the start of every call. Calls that overlap on the GPU (different streams running at the same
-// time) race on the array and must be serialised by the caller.
+// time) race on the array and must be serialised by the caller. The array's address is looked
+// up once per CUDA context, on the first call made with that context current; that first call
+// must come before any stream capture.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -32,10 +35,64 @@ struct NoallocScratch {
 
 static __device__ __align__(256) NoallocScratch g_noalloc_scratch;
 
-// Device address of g_noalloc_scratch per device, resolved once per device (with that device
-// current) by cudaGetSymbolAddress; host code never hands the symbol itself to a kernel.
-NoallocScratch* g_scratch_addr[kMaxDevices] = {};
+// Device address of g_noalloc_scratch, resolved by cudaGetSymbolAddress once per CUDA context
+// (with that context current) and cached under the context's process-unique ID, so that a
+// non-primary context on the same device, or a primary context re-created after
+// cudaDeviceReset, resolves its own module instance instead of reusing a stale address.
+constexpr int kMaxContexts = 4 * kMaxDevices;
+struct ScratchEntry {
+  unsigned long long ctx_id;
+  NoallocScratch* addr;
+};
+ScratchEntry g_scratch_cache[kMaxContexts];
+int g_scratch_count = 0;
 std::mutex g_scratch_mu;
+
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+
+// ID of the current CUDA context (0 when none is current or the driver lacks the query)
+unsigned long long current_context_id() {
+  static PfnCtxGetCurrent get_current = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    looked_up = true;
+    cudaDriverEntryPointQueryResult q;
+    void* fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<PfnCtxGetCurrent>(fn);
+    fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PfnCtxGetId>(fn);
+    cudaGetLastError();
+  }
+  if (!get_current || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+  if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// The scratch address for the current context; nullptr on a CUDA error.
+NoallocScratch* scratch_address() {
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  unsigned long long id = current_context_id();
+  if (id)
+    for (int i = 0; i < g_scratch_count; i++)
+      if (g_scratch_cache[i].ctx_id == id) return g_scratch_cache[i].addr;
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (!id) id = current_context_id();  // the runtime may have just made the primary current
+  if (id && g_scratch_count < kMaxContexts) g_scratch_cache[g_scratch_count++] = {id, (NoallocScratch*)p};
+  return static_cast<NoallocScratch*>(p);
+}
 
 __global__ void __launch_bounds__(glia::kThreads)
     k_mismatch_noalloc(const float* __restrict__ c, const float* __restrict__ O,
@@ -61,24 +118,8 @@ extern "C" int glia_mismatch_f32_noalloc(const float* c, const float* obs, const
                                          float* pt, int64_t n, double* sumsq, void* stream) {
   if (!c || !obs || !d || !sumsq || n < 1) return GLIA_ERR_INVALID;
   if (n > (int64_t)kMaxTiles * kTile) return GLIA_ERR_INVALID;  // beyond the scratch capacity
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-    cudaGetLastError();
-    return GLIA_ERR_NO_DEVICE;
-  }
-  NoallocScratch* scratch;
-  {
-    std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
-      void* p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
-        cudaGetLastError();
-        return GLIA_ERR_CUDA;
-      }
-      g_scratch_addr[dev] = static_cast<NoallocScratch*>(p);
-    }
-    scratch = g_scratch_addr[dev];
-  }
+  NoallocScratch* scratch = scratch_address();
+  if (!scratch) return GLIA_ERR_CUDA;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (cudaMemsetAsync(&scratch->counter, 0, sizeof(unsigned int), s) != cudaSuccess) {
     cudaGetLastError();

@@ -220,14 +220,21 @@ __global__ void __launch_bounds__(256, 2)
     }
     cp_async_commit();
   };
-  // the slot's rows have landed (uniform result); on a timeout record the fault and wait, bounded,
-  // for the other slot's copies
-  auto ready = [&](int which, int it) {
+  // The slot's rows of tile `it` (phase `it` of its barrier) have landed (uniform result). On a
+  // timeout: record the fault and wait, bounded, for every copy of this CTA still in flight — the
+  // late phase itself and the other slot's outstanding phase. When slot 0 is late, slot 1 holds
+  // phase `it` (staged one tile ahead). When slot 1 is late, slot 0 was already re-staged for the
+  // next tile during this tile's G_x transform: phase it + 1, pending only if that tile exists.
+  auto ready = [&](int which, int it, bool next) {
     const bool ok = threadIdx.x != 0 || mbar_wait(&bars[which], (unsigned)(it & 1));
     if (!__syncthreads_or(!ok)) return true;
     if (threadIdx.x == 0) {
       atomicExch(&sc->dev_fault, 1);
-      mbar_wait(&bars[which ^ 1], (unsigned)(it & 1));
+      mbar_wait(&bars[which], (unsigned)(it & 1));
+      if (which == 0)
+        mbar_wait(&bars[1], (unsigned)(it & 1));
+      else if (next)
+        mbar_wait(&bars[0], (unsigned)((it + 1) & 1));
     }
     cp_async_wait<0>();
     __syncthreads();
@@ -239,8 +246,9 @@ __global__ void __launch_bounds__(256, 2)
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, it++) {
     const int x = tile / CB, kz = (tile - x * CB) * T + c;
     const bool pk = kz == 0;
+    const bool next = tile + (int)gridDim.x < ntiles;
     cp_async_wait<1>();  // nyq of G_x
-    if (!ready(0, it)) return;
+    if (!ready(0, it, next)) return;
     xdft<D, +1>(
         sm, tw, c, gi,
         [&](int, int b, int a) {
@@ -255,7 +263,7 @@ __global__ void __launch_bounds__(256, 2)
         [&] { stage(slGx, nyq, Gx, tile + gridDim.x, &bars[0]); },
         [&](int, int k1, int k2, float2 y) { H[(x * NN + k1 + R1 * k2) * NQ + kz] = y; });
     cp_async_wait<1>();  // nyq of G_0
-    if (!ready(1, it)) return;
+    if (!ready(1, it, next)) return;
     float2 v[NB1][R1];
 #pragma unroll
     for (int m = 0; m < NB1; m++) {

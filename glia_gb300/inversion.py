@@ -2,13 +2,29 @@
 
 Restates the reference's optimizer set-up (src/opt/Optimizer.cpp:116-286,
 src/opt/TILOptimizer.cpp:245-272, src/opt/TaoInterface.cpp:362-530): TAO BLMVM (bounded
-limited-memory variable metric) with 10 correction pairs, at most 10 function evaluations per line
-search, stopping when the projected-gradient norm falls below gttol * ||g_0|| (gttol = 1e-3) or
-below gatol (1e-4), or after newton_maxit (30) iterations; bounds p >= 0, kappa in [1e-3, 1],
-rho in [1, 15]. The search direction is the two-loop L-BFGS product with the scalar initial
-scaling s'y / y'y, projected onto the free variables; the step is a projected backtracking
-(Armijo) line search along P(x + a d). All vectors are FP64 on the host; each objective and
-gradient is one glia_eval_objective[_and_gradient] call.
+limited-memory variable metric) with 10 correction pairs (lbfgs_vectors_), at most 10 function
+evaluations per line search (ls_max_func_evals), stopping when the projected-gradient norm falls
+below gttol * ||g_0|| (opttolgrad_ = 1e-3) or below gatol (1e-4), or after newton_maxit (30)
+iterations; bounds p >= 0, kappa in [1e-3, 1], rho in [1, 15].
+
+PETSc/TAO (3.7-3.11) is not part of the reference tree; its published algorithms are restated:
+- line search (OptimizerSettings::linesearch_, default MT, include/Parameters.h:36): the
+  More-Thuente search of MINPACK-2 (dcsrch / dcstep; J. J. More and D. J. Thuente, "Line search
+  algorithms with guaranteed sufficient decrease", ACM TOMS 20, 1994) with ftol 1e-4, gtol 0.9,
+  xtol 1e-10, minimum step = machine epsilon (ls_minstep_, Optimizer.cpp:153-155), initial step
+  1 (:163); on a bounded problem each trial point is projected onto the box and the directional
+  derivative is taken along the projected path, g(x_t) . (x_t - x) / t. ARMIJO: projected
+  backtracking with sufficient decrease 1e-4 and halving.
+- initial inverse Hessian of the two-loop recursion (lbfgs_scale_type_, Optimizer.cpp:180-192 for
+  PETSc >= 3.9, default "diagonal"; :225-230 for older PETSc: Broyden scalar scaling with a
+  history of 5): "none" (identity), "scalar" (s'y / y'y summed over the last `scale_hist`
+  pairs, lbfgs_scale_hist_ = 5), "diagonal" (a diagonal BFGS update of the initial matrix per
+  pair, J. C. Gilbert and C. Lemarechal, Math. Programming 45, 1989: with B = D^-1,
+  B_i <- B_i + y_i^2 / y's - (B_i s_i)^2 / s'Bs, entries kept positive, started from the scalar
+  scaling of the first pair).
+The direction is the two-loop product on the gradient, with the variables held at a bound (and
+those the step would push out of the box) removed. All vectors are FP64 on the host; each
+objective and gradient is one glia_eval_objective[_and_gradient] call.
 
     python -m glia_gb300.inversion --n 128      # the 128^3 reconstruction, mixed vs FP64
 """
@@ -21,6 +37,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+EPS = float(np.finfo(np.float64).eps)
+
 
 @dataclass
 class LbfgsSettings:
@@ -29,8 +47,16 @@ class LbfgsSettings:
     gatol: float = 1e-4         # gatol_
     maxit: int = 30             # newton_maxit_
     ls_max_funcs: int = 10      # ls_max_func_evals
+    line_search: str = "mt"     # linesearch_: "mt" (More-Thuente) or "armijo"
+    scale_type: str = "diagonal"  # lbfgs_scale_type_: "none", "scalar", "diagonal"
+    scale_hist: int = 5         # lbfgs_scale_hist_
     armijo_c1: float = 1e-4
     shrink: float = 0.5
+    mt_ftol: float = 1e-4
+    mt_gtol: float = 0.9
+    mt_xtol: float = 1e-10
+    ls_minstep: float = EPS     # ls_minstep_
+    ls_maxstep: float = 1e20
 
 
 @dataclass
@@ -53,6 +79,185 @@ def projected_gradient(x, g, lb, ub):
     return pg
 
 
+# ------------------------------------------------------------------------------------------
+# More-Thuente line search (MINPACK-2 dcstep / dcsrch, restated)
+# ------------------------------------------------------------------------------------------
+def dcstep(stx, fx, dx, sty, fy, dy, stp, fp, dp, brackt, stpmin, stpmax):
+    """One safeguarded step of the interval of uncertainty [stx, sty] (cubic / quadratic / secant
+    interpolation, four cases). Returns (stx, fx, dx, sty, fy, dy, stp, brackt)."""
+    sgnd = dp * np.sign(dx)
+    if fp > fx:  # 1: higher value, the minimum is bracketed
+        theta = 3.0 * (fx - fp) / (stp - stx) + dx + dp
+        s = max(abs(theta), abs(dx), abs(dp))
+        gamma = s * np.sqrt(max(0.0, (theta / s) ** 2 - (dx / s) * (dp / s)))
+        if stp < stx:
+            gamma = -gamma
+        p = (gamma - dx) + theta
+        q = ((gamma - dx) + gamma) + dp
+        stpc = stx + (p / q) * (stp - stx)
+        stpq = stx + ((dx / ((fx - fp) / (stp - stx) + dx)) / 2.0) * (stp - stx)
+        stpf = stpc if abs(stpc - stx) < abs(stpq - stx) else stpc + (stpq - stpc) / 2.0
+        brackt = True
+    elif sgnd < 0.0:  # 2: lower value, derivatives of opposite sign
+        theta = 3.0 * (fx - fp) / (stp - stx) + dx + dp
+        s = max(abs(theta), abs(dx), abs(dp))
+        gamma = s * np.sqrt(max(0.0, (theta / s) ** 2 - (dx / s) * (dp / s)))
+        if stp > stx:
+            gamma = -gamma
+        p = (gamma - dp) + theta
+        q = ((gamma - dp) + gamma) + dx
+        stpc = stp + (p / q) * (stx - stp)
+        stpq = stp + (dp / (dp - dx)) * (stx - stp)
+        stpf = stpc if abs(stpc - stp) > abs(stpq - stp) else stpq
+        brackt = True
+    elif abs(dp) < abs(dx):  # 3: lower value, same sign, derivative decreases in magnitude
+        theta = 3.0 * (fx - fp) / (stp - stx) + dx + dp
+        s = max(abs(theta), abs(dx), abs(dp))
+        gamma = s * np.sqrt(max(0.0, (theta / s) ** 2 - (dx / s) * (dp / s)))
+        if stp > stx:
+            gamma = -gamma
+        p = (gamma - dp) + theta
+        q = (gamma + (dx - dp)) + gamma
+        r = p / q
+        if r < 0.0 and gamma != 0.0:
+            stpc = stp + r * (stx - stp)
+        elif stp > stx:
+            stpc = stpmax
+        else:
+            stpc = stpmin
+        stpq = stp + (dp / (dp - dx)) * (stx - stp)
+        if brackt:
+            stpf = stpc if abs(stpc - stp) < abs(stpq - stp) else stpq
+            if stp > stx:
+                stpf = min(stp + 0.66 * (sty - stp), stpf)
+            else:
+                stpf = max(stp + 0.66 * (sty - stp), stpf)
+        else:
+            stpf = stpc if abs(stpc - stp) > abs(stpq - stp) else stpq
+            stpf = min(stpmax, max(stpmin, stpf))
+    else:  # 4: lower value, same sign, derivative does not decrease
+        if brackt:
+            theta = 3.0 * (fp - fy) / (sty - stp) + dy + dp
+            s = max(abs(theta), abs(dy), abs(dp))
+            gamma = s * np.sqrt(max(0.0, (theta / s) ** 2 - (dy / s) * (dp / s)))
+            if stp > sty:
+                gamma = -gamma
+            p = (gamma - dp) + theta
+            q = ((gamma - dp) + gamma) + dy
+            stpf = stp + (p / q) * (sty - stp)
+        elif stp > stx:
+            stpf = stpmax
+        else:
+            stpf = stpmin
+    if fp > fx:
+        sty, fy, dy = stp, fp, dp
+    else:
+        if sgnd < 0.0:
+            sty, fy, dy = stx, fx, dx
+        stx, fx, dx = stp, fp, dp
+    return stx, fx, dx, sty, fy, dy, stpf, brackt
+
+
+def more_thuente(phi, f0, g0, stp, s: LbfgsSettings):
+    """MINPACK-2 dcsrch: a step satisfying f(t) <= f0 + ftol t g0 and |f'(t)| <= gtol |g0|.
+    phi(t) -> (f, f'(t), payload). Returns (t, f, payload, evaluations, converged); payload is
+    that of the returned step (None when no evaluation was kept)."""
+    xtrapl, xtrapu = 1.1, 4.0
+    ftol, gtol, xtol = s.mt_ftol, s.mt_gtol, s.mt_xtol
+    stpmin, stpmax = s.ls_minstep, s.ls_maxstep
+    if g0 >= 0.0:
+        return 0.0, f0, None, 0, False
+    brackt, stage = False, 1
+    gtest = ftol * g0
+    width = stpmax - stpmin
+    width1 = 2.0 * width
+    stx, fx, gx = 0.0, f0, g0
+    sty, fy, gy = 0.0, f0, g0
+    stmin, stmax = 0.0, stp + xtrapu * stp
+    best = (0.0, f0, None)
+    for nfev in range(1, s.ls_max_funcs + 1):
+        stp = min(max(stp, stpmin), stpmax)
+        f, g, payload = phi(stp)
+        ftest = f0 + stp * gtest
+        if f <= ftest and f < best[1]:
+            best = (stp, f, payload)
+        if stage == 1 and f <= ftest and g >= 0.0:
+            stage = 2
+        if f <= ftest and abs(g) <= gtol * (-g0):
+            return stp, f, payload, nfev, True
+        if (brackt and (stp <= stmin or stp >= stmax)) or (brackt and stmax - stmin <= xtol * stmax) \
+                or (stp == stpmax and f <= ftest and g <= gtest) \
+                or (stp == stpmin and (f > ftest or g >= gtest)):
+            break  # rounding errors, interval below xtol, or a step bound reached
+        if stage == 1 and f <= fx and f > ftest:  # modified function psi(t) = f(t) - f0 - t gtest
+            fm, fxm, fym = f - stp * gtest, fx - stx * gtest, fy - sty * gtest
+            gm, gxm, gym = g - gtest, gx - gtest, gy - gtest
+            stx, fxm, gxm, sty, fym, gym, stp, brackt = dcstep(stx, fxm, gxm, sty, fym, gym, stp,
+                                                                fm, gm, brackt, stmin, stmax)
+            fx, fy = fxm + stx * gtest, fym + sty * gtest
+            gx, gy = gxm + gtest, gym + gtest
+        else:
+            stx, fx, gx, sty, fy, gy, stp, brackt = dcstep(stx, fx, gx, sty, fy, gy, stp, f, g,
+                                                            brackt, stmin, stmax)
+        if brackt:
+            if abs(sty - stx) >= 0.66 * width1:
+                stp = stx + 0.5 * (sty - stx)
+            width1 = width
+            width = abs(sty - stx)
+            stmin, stmax = min(stx, sty), max(stx, sty)
+        else:
+            stmin = stp + xtrapl * (stp - stx)
+            stmax = stp + xtrapu * (stp - stx)
+        stp = min(max(stp, stpmin), stpmax)
+        if (brackt and (stp <= stmin or stp >= stmax)) or (brackt and stmax - stmin <= xtol * stmax):
+            stp = stx
+    # no step met both conditions: keep the best sufficient-decrease step, if any
+    t, f, payload = best
+    return t, f, payload, nfev, False
+
+
+# ------------------------------------------------------------------------------------------
+# L-BFGS initial inverse Hessian
+# ------------------------------------------------------------------------------------------
+class InitialScaling:
+    """H0 of the two-loop recursion: identity, scalar (s'y / y'y over the last `hist` pairs) or
+    diagonal (Gilbert-Lemarechal diagonal BFGS update of B0 = H0^-1, per accepted pair)."""
+
+    def __init__(self, kind: str, n: int, hist: int):
+        if kind not in ("none", "scalar", "diagonal"):
+            raise ValueError(f"unknown scale type {kind}")
+        self.kind, self.hist = kind, max(1, hist)
+        self.pairs = []
+        self.B = None  # diagonal of the initial Hessian (diagonal kind)
+        self.n = n
+
+    def update(self, sv, yv):
+        self.pairs.append((float(sv @ yv), float(yv @ yv)))
+        self.pairs = self.pairs[-self.hist:]
+        if self.kind != "diagonal":
+            return
+        sy = float(sv @ yv)
+        if self.B is None:
+            self.B = np.full(self.n, float(yv @ yv) / sy)  # start at the scalar scaling
+        sBs = float(sv @ (self.B * sv))
+        newB = self.B + yv * yv / sy - (self.B * sv) ** 2 / sBs
+        ok = np.isfinite(newB) & (newB > 1e-12 * np.max(self.B))
+        self.B = np.where(ok, newB, self.B)
+
+    def reset(self):
+        self.pairs.clear()
+        self.B = None
+
+    def apply(self, q, gnorm):
+        if not self.pairs:  # no curvature yet: a step of unit length along the gradient
+            return q / max(gnorm, 1e-300)
+        if self.kind == "none":
+            return q.copy()
+        if self.kind == "scalar":
+            return q * (sum(p[0] for p in self.pairs) / sum(p[1] for p in self.pairs))
+        return q / self.B
+
+
 def bounded_lbfgs(fun_grad, fun, x0, lb, ub, s: LbfgsSettings = LbfgsSettings()) -> LbfgsResult:
     """Minimise fun over lb <= x <= ub. fun_grad(x) -> (J, g); fun(x) -> J."""
     x = np.clip(np.asarray(x0, dtype=np.float64), lb, ub)
@@ -61,6 +266,7 @@ def bounded_lbfgs(fun_grad, fun, x0, lb, ub, s: LbfgsSettings = LbfgsSettings())
     pg = projected_gradient(x, g, lb, ub)
     g0 = float(np.linalg.norm(pg)) or 1.0
     S, Y = [], []
+    H0 = InitialScaling(s.scale_type, x.size, s.scale_hist)
     hist = [{"it": 0, "J": J, "gnorm": g0}]
     reason = "maxit"
     it = 0
@@ -82,8 +288,7 @@ def bounded_lbfgs(fun_grad, fun, x0, lb, ub, s: LbfgsSettings = LbfgsSettings())
             a = rho * (sv @ q)
             q -= a * yv
             alphas.append((rho, a))
-        gamma = (S[-1] @ Y[-1]) / (Y[-1] @ Y[-1]) if S else 1.0 / max(gn, 1e-300)
-        r = gamma * q
+        r = H0.apply(q, gn)
         for (sv, yv), (rho, a) in zip(zip(S, Y), reversed(alphas)):
             b = rho * (yv @ r)
             r += (a - b) * sv
@@ -95,33 +300,46 @@ def bounded_lbfgs(fun_grad, fun, x0, lb, ub, s: LbfgsSettings = LbfgsSettings())
         if not d @ pg < 0:  # not a descent direction: restart from the projected gradient
             S.clear()
             Y.clear()
+            H0.reset()
             d = -pg / max(gn, 1e-300)
-        # projected backtracking line search; the first trial also takes the gradient (it is
-        # accepted in most iterations), later trials take the objective only
-        step, accepted, gnew = 1.0, False, None
-        for trial in range(s.ls_max_funcs):
-            xn = np.clip(x + step * d, lb, ub)
-            if trial == 0:
+        if s.line_search == "mt":
+            def phi(t):
+                xt = np.clip(x + t * d, lb, ub)
+                Jt, gt = fun_grad(xt)
+                return Jt, float(gt @ (xt - x)) / t, (xt, Jt, gt)
+
+            step, Jn, payload, nfev, ok = more_thuente(phi, J, float(g @ d), 1.0, s)
+            fevals += nfev
+            gevals += nfev
+            accepted = payload is not None and Jn < J
+            if accepted:
+                xn, Jn, gnew = payload
+        else:
+            step, accepted, gnew = 1.0, False, None
+            for trial in range(s.ls_max_funcs):
+                xn = np.clip(x + step * d, lb, ub)
+                if trial == 0:
+                    Jn, gnew = fun_grad(xn)
+                    gevals += 1
+                else:
+                    Jn, gnew = fun(xn), None
+                fevals += 1
+                if Jn <= J + s.armijo_c1 * (g @ (xn - x)):
+                    accepted = True
+                    break
+                step *= s.shrink
+            if accepted and gnew is None:
                 Jn, gnew = fun_grad(xn)
+                fevals += 1
                 gevals += 1
-            else:
-                Jn, gnew = fun(xn), None
-            fevals += 1
-            if Jn <= J + s.armijo_c1 * (g @ (xn - x)):
-                accepted = True
-                break
-            step *= s.shrink
         if not accepted:
             reason = "linesearch"
             break
-        if gnew is None:
-            Jn, gnew = fun_grad(xn)
-            fevals += 1
-            gevals += 1
         sv, yv = xn - x, gnew - g
         if sv @ yv > 1e-12 * np.linalg.norm(sv) * np.linalg.norm(yv):
             S.append(sv)
             Y.append(yv)
+            H0.update(sv, yv)
             if len(S) > s.m:
                 S.pop(0)
                 Y.pop(0)

@@ -8,7 +8,9 @@
 //   initializeGrid                                    src/grad/SpectralOperators.cpp:424-446
 //   DiffCoef::setValues / setValuesSinusoidal         src/mat/DiffCoef.cpp:77-187
 //   DiffusionSolver::precFactor / solve               src/pde/DiffusionSolver.cpp:119-250
-//   Tumor (c_0_, c_t_, p_0_, p_t_)                    src/mat/Tumor.cpp:3-57
+//   Tumor (c_0_, c_t_, p_0_, p_t_), setSinusoidalCoefficients
+//                                                     src/mat/Tumor.cpp:3-57, 102-112
+//   DerivativeOperators::updateReactionAndDiffusion   src/grad/DerivativeOperators.cpp:323-367
 //   PdeOperatorsRD::solveState / solveAdjoint         src/pde/PdeOperators.cpp:235-420
 //   DerivativeOperatorsRD::evaluateObjective / evaluateGradient /
 //                          evaluateObjectiveAndGradient src/grad/DerivativeOperatorsRD.cpp:7-226
@@ -178,6 +180,15 @@ class Tumor {
     return glia_set_phi(spec_ops_->ctx_, cm.data(), (int)(cm.size() / 3), tu.phi_sigma_,
                         tu.smoothing_factor_);
   }
+  // Tumor::setSinusoidalCoefficients (src/mat/Tumor.cpp:102-112): sinusoidal tissue, then
+  // k_->setValues and rho_->setValues from the parameters
+  PetscErrorCode setSinusoidalCoefficients(std::shared_ptr<Parameters> params) {
+    int rc = glia_set_tissue_sinusoidal(spec_ops_->ctx_);
+    if (rc) return rc;
+    auto& tu = *params->tu_;
+    return glia_set_coefficients(spec_ops_->ctx_, tu.k_, tu.k_gm_wm_ratio_, tu.k_glm_wm_ratio_,
+                                 tu.rho_, tu.r_gm_wm_ratio_, tu.r_glm_wm_ratio_);
+  }
   Vec c_0_, c_t_, p_0_, p_t_;
   std::shared_ptr<Parameters> params_;
   std::shared_ptr<SpectralOperators> spec_ops_;
@@ -246,9 +257,37 @@ class DerivativeOperatorsRD {
   DerivativeOperatorsRD(std::shared_ptr<PdeOperatorsRD> pde, std::shared_ptr<Parameters> p,
                         std::shared_ptr<Tumor> t)
       : pde_operators_(pde), params_(p), tumor_(t) {}
+  // the optimizer settings and, when the parameters hold no p (flag_reaction_inv_: the
+  // objective starts from Tumor::c_0_ instead of Phi p), the initial condition
   PetscErrorCode sync_settings() {
     glia_opt_settings s = to_opt(*params_, all_gradients_);
-    return glia_set_opt(ctx(), &s);
+    int rc = glia_set_opt(ctx(), &s);
+    if (!rc && params_->opt_->flag_reaction_inv_) rc = glia_set_c0(ctx(), tumor_->c_0_.data());
+    return rc;
+  }
+  // DerivativeOperators::updateReactionAndDiffusion (src/grad/DerivativeOperators.cpp:323-367)
+  // with DiffCoef / ReacCoef::updateIsotropicCoefficients (src/mat/DiffCoef.cpp:60-75,
+  // src/mat/ReacCoef.cpp:40-50): k1 = x[np] k_scale, k2, k3 from x[np + 1], x[np + 2] when
+  // nk > 1 (ratios k2 / k1, k3 / k1), else the parameters' ratios; rho likewise from x[np + nk]
+  // under flag_reaction_inv_. Coefficients that are not inverted come from the parameters.
+  PetscErrorCode updateReactionAndDiffusion(const Vec& x) {
+    auto& tu = *params_->tu_;
+    auto& op = *params_->opt_;
+    const int np = tu.np_, nk = tu.nk_, nr = tu.nr_;
+    if ((int)x.size() < np + nk + (op.flag_reaction_inv_ ? nr : 0)) return GLIA_ERR_INVALID;
+    double k = tu.k_, kg = tu.k_gm_wm_ratio_, kc = tu.k_glm_wm_ratio_;
+    if (op.diffusivity_inversion_ || op.flag_reaction_inv_) {
+      k = x[np] * op.k_scale_;
+      if (nk > 1) kg = x[np + 1] * op.k_scale_ / k;
+      if (nk > 2) kc = x[np + 2] * op.k_scale_ / k;
+    }
+    double r = tu.rho_, rg = tu.r_gm_wm_ratio_, rc = tu.r_glm_wm_ratio_;
+    if (op.flag_reaction_inv_) {
+      r = x[np + nk] * op.rho_scale_;
+      if (nr > 1) rg = x[np + nk + 1] * op.rho_scale_ / r;
+      if (nr > 2) rc = x[np + nk + 2] * op.rho_scale_ / r;
+    }
+    return glia_set_coefficients(ctx(), k, kg, kc, r, rg, rc);
   }
   // the t = 0 data of the two-snapshot objective, or back to one snapshot
   PetscErrorCode sync_data(const Data& data) {

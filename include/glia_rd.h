@@ -251,8 +251,9 @@ int glia_get_timing(glia_ctx* ctx, int slot, const char** name, int64_t* launche
  * pointers (float fields, one double result); work is ordered on `stream` (NULL = the legacy
  * default stream). It needs no context and calls no allocator: its reduction scratch is a
  * static 64 KiB device array shared by every call, which limits n to 2^29 voxels (larger n
- * returns GLIA_ERR_INVALID). The first call on each device resolves that array's address
- * (cudaGetSymbolAddress) and must come before any stream capture. Calls that overlap on the GPU
+ * returns GLIA_ERR_INVALID). The first call in each CUDA context (the device's primary context,
+ * or any other context current at the call) resolves that array's address with
+ * cudaGetSymbolAddress and must come before any stream capture. Calls that overlap on the GPU
  * race on the shared scratch; serialise them. */
 int glia_mismatch_f32_noalloc(const float* c, const float* obs, const float* d, float* pt,
                               int64_t n, double* sumsq, void* stream);

@@ -57,3 +57,54 @@ def test_phi_backward_is_phi_transpose():
     (ga.phi_apply(p, ctx) * v).sum().backward()
     c = ctx.phi_apply(np.eye(4)[2])
     assert float(p.grad[2]) == pytest.approx(float(c @ v.numpy()), rel=1e-12)
+
+
+def test_solve_state_backward_after_other_calls_on_the_context():
+    """A gradient evaluation (and a coefficient change and back) between the forward and the
+    backward of solve_state rewrites the context's state history; the backward must still be
+    the adjoint around the forward's own states."""
+    ctx, wl, tissue, centers = _ctx(nt=3)
+    n = 32
+    rng = np.random.default_rng(2)
+    g = torch.tensor(rng.standard_normal(n ** 3))
+    c0_np = ctx.phi_apply(np.array([0.6, 0.0, 0.3, 0.9]))
+
+    c0 = torch.tensor(c0_np, requires_grad=True)
+    (ga.solve_state(c0, ctx) * g).sum().backward()
+    clean = c0.grad.clone()
+
+    c0 = torch.tensor(c0_np, requires_grad=True)
+    c1 = ga.solve_state(c0, ctx)
+    d1 = observation(wl, tissue, centers)
+    x = torch.tensor(np.concatenate([[0.9, 0.9, 0.9, 0.9], [wl.kappa, wl.rho]]),
+                     requires_grad=True)
+    ga.rd_objective(x, ctx, d1).backward()          # another forward + adjoint sweep
+    ctx.set_coefficients(k=wl.kappa * 3, rho=wl.rho, k_gm_wm=wl.k_gm_wm)
+    ctx.solve_state(c0_np * 0.5)
+    ctx.set_coefficients(k=wl.kappa, rho=wl.rho, k_gm_wm=wl.k_gm_wm)
+    (c1 * g).sum().backward()
+    assert np.array_equal(c0.grad.numpy(), clean.numpy())
+
+
+def test_context_generation_advances_on_history_writes_only():
+    ctx, wl, *_ = _ctx(nt=2)
+    g0 = ctx.generation
+    ctx.stats()
+    ctx.phi_apply(np.array([0.1, 0.2, 0.3, 0.4]))
+    assert ctx.generation == g0
+    ctx.solve_state(ctx.phi_apply(np.array([0.1, 0.2, 0.3, 0.4])))
+    assert ctx.generation == g0 + 1
+    p0 = ctx.phi_generation
+    ctx.set_coefficients(k=wl.kappa, rho=wl.rho)
+    assert ctx.phi_generation == p0 and ctx.generation == g0 + 2
+    ctx.set_opt(phi_store=1)
+    assert ctx.phi_generation == p0 + 1
+
+
+def test_phi_backward_refuses_a_changed_basis():
+    ctx, *_ = _ctx()
+    p = torch.tensor([0.3, 0.1, 0.0, 0.8], dtype=torch.float64, requires_grad=True)
+    c = ga.phi_apply(p, ctx)
+    ctx.set_opt(phi_store=0)
+    with pytest.raises(RuntimeError, match="changed since the forward"):
+        c.sum().backward()

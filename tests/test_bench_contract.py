@@ -30,6 +30,18 @@ def test_reference_arm_prints_one_contract_line():
     assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is True
     assert d["unit"] == "gradient evals/s" and d["steps"] == 1 and d["warmup"] == 0
     assert d["config"]["n"] == 32 and "workload" in d["config"]
+    # the config is the workload only (the same dict the GPU arm prints), the arm is named outside
+    sys.path.insert(0, ROOT)
+    import bench
+
+    class A:
+        n, nt, n_gauss = 32, 2, 8
+    assert d["config"] == bench.workload_config(A)
+    assert "arm" not in d["config"] and d["arm"]
+    # each step is one full oracle evaluation at nt_per_step steps; value extrapolates it
+    ex = d["extrapolated"]
+    assert ex["nt_per_step"] == 1 and ex["nt_per_evaluation"] == 2
+    assert abs(1.0 / d["value"] - d["ms_per_step"] * 1e-3 * 2) <= 1e-9 / d["value"]
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,

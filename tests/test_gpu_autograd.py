@@ -60,3 +60,39 @@ def test_solve_state_backward_on_gpu_is_the_adjoint():
     cm = g.solve_state(c0.detach().numpy() - h * v)
     assert float(w.numpy() @ ((cp - cm) / (2 * h))) == pytest.approx(float(c0.grad.numpy() @ v),
                                                                      rel=1e-6)
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+def test_device_path_equals_host_path_bit_for_bit(prec):
+    """CUDA-tensor arguments go to the library as device pointers on the caller's stream; the
+    results equal those of host float64 buffers exactly (same conversions, same kernels)."""
+    g, d1, x0, np_ = _setup(prec)
+    n = 32
+    rng = np.random.default_rng(5)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        x = torch.tensor(x0, requires_grad=True)
+        Jh = ga.rd_objective(x, g, d1)
+        Jh.backward()
+        gh = x.grad.clone()
+        x = torch.tensor(x0, requires_grad=True)
+        Jd = ga.rd_objective(x, g, torch.tensor(d1, device="cuda"))
+        Jd.backward()
+        assert Jh.item() == Jd.item()
+        assert torch.equal(gh, x.grad)
+
+        w = torch.tensor(rng.standard_normal(n ** 3))
+        c0h = torch.tensor(g.phi_apply(x0[:np_]), requires_grad=True)
+        c1h = ga.solve_state(c0h, g)
+        (c1h * w).sum().backward()
+        c0d = c0h.detach().cuda().requires_grad_()
+        c1d = ga.solve_state(c0d, g)
+        (c1d * w.cuda()).sum().backward()
+        assert torch.equal(c1h, c1d.cpu())
+        assert torch.equal(c0h.grad, c0d.grad.cpu())
+        if prec == MIXED:  # float32 tensors: no conversion on the way in, exact on the way out
+            c1f = ga.solve_state(c0h.detach().to("cuda", torch.float32), g)
+            assert c1f.dtype == torch.float32
+            assert torch.equal(c1f.cpu(), c1h.detach().to(torch.float32))
+    s.synchronize()
+    assert g.ptr_mode == 0 and g.stream == 0  # the context's own modes are restored
