@@ -135,7 +135,18 @@ SIGNATURES = {
                                      c_void_p]),
     "get_timing": (c_int, [_CTX, c_int, POINTER(c_char_p), POINTER(c_int64), POINTER(c_double),
                            POINTER(c_double)]),
+    "batch_create": (c_int, [POINTER(c_void_p), c_int, POINTER(c_void_p)]),
+    "batch_capture": (c_int, [c_void_p, POINTER(_D), POINTER(c_int), POINTER(c_void_p),
+                              POINTER(c_int)]),
+    "batch_launch": (c_int, [c_void_p, c_void_p]),
+    "batch_results": (c_int, [c_void_p, c_void_p, _D, POINTER(_D)]),
+    "batch_last_error": (c_char_p, [c_void_p]),
+    "batch_destroy": (c_int, [c_void_p]),
 }
+
+# entry points of the CUDA library only (the oracle evaluates one problem per call)
+BATCH_NAMES = ("batch_create", "batch_capture", "batch_launch", "batch_results",
+               "batch_last_error", "batch_destroy")
 
 
 class Bound:

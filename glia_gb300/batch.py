@@ -1,13 +1,16 @@
 """Batched uneven gradient evaluations: many independent problems of different grid sizes
 sharing one GPU.
 
-Each problem owns a context (its own CUDA stream, cuFFT plans, PCG graph). A pool of host
-threads feeds the contexts (the C-ABI calls release the GIL), so up to `concurrency` problems are
-in flight at once and the GPU overlaps their kernels; inside each problem the PCG loops run as
-device-side graphs, so the threads issue work and wait on one small read per sweep. The schedule
-(concurrency, launch geometry per grid size, longest-first order) is chosen by `autotune`, which
-measures candidate schedules on a shortened copy of the batch and caches the winner in a JSON
-file keyed by the batch's shape.
+Each problem owns a context (its own CUDA stream, cuFFT plans, PCG graph). Two ways to run them:
+- one CUDA graph (`GraphBatch`, glia_batch_* of the C-ABI): every problem's forward, adjoint and
+  gradient sweeps, with their PCG loops as conditional WHILE nodes, captured as parallel branches
+  of one graph that is launched once; branches are ordered in groups (contexts of one group run
+  concurrently, groups one after another);
+- host threads (`Batch.evaluate`): a pool feeds up to `concurrency` contexts at once (the C-ABI
+  calls release the GIL); inside each problem the PCG loops run as device-side graphs.
+The schedule (launch geometry per grid size; branch grouping for the graph, concurrency for the
+threads) is chosen by `autotune_graph` / `autotune`, which measure candidate schedules on a
+shortened copy of the batch and cache the winner in a JSON file keyed by the batch's shape.
 
 The default batch: 32 problems, 16 at 64^3, 12 at 128^3 and 4 at 256^3; problem b has tissue seed
 1000 + b, rho ~ U[4, 15], kappa ~ U[0.005, 0.1], 64 / 216 / 512 Gaussians (by grid) with 5 % active,
@@ -119,6 +122,131 @@ class Batch:
             c.close()
 
 
+class GraphBatch:
+    """A Batch's evaluations as one CUDA graph (glia_batch_capture / launch / results). Each
+    context first runs one ordinary evaluation (plans and per-context PCG graphs are created
+    there; `reference` keeps those results), then the graph is captured at the problems' x and
+    data. The launch geometry must be set before construction: it is part of the graph."""
+
+    def __init__(self, batch: "Batch", group=None):
+        import ctypes
+
+        from .native import load
+
+        self.batch = batch
+        self.api = load()
+        n = len(batch.ctxs)
+        self.reference = [c.eval_objective_and_gradient(p.x, d)
+                          for c, p, d in zip(batch.ctxs, batch.problems, batch.data)]
+        hs = (ctypes.c_void_p * n)(*[c._h.value for c in batch.ctxs])
+        self.h = ctypes.c_void_p()
+        self._check(self.api.batch_create(hs, n, ctypes.byref(self.h)), "batch_create")
+        self.capture(group)
+
+    def _check(self, rc, where):
+        if rc != 0:
+            from .context import GliaError
+
+            msg = self.api.batch_last_error(self.h) if self.h else b""
+            raise GliaError(rc, where, msg.decode() if msg else "")
+
+    def capture(self, group=None):
+        import ctypes
+
+        b = self.batch
+        n = len(b.ctxs)
+        self._xs = [np.ascontiguousarray(p.x, dtype=np.float64) for p in b.problems]
+        self._ds = [np.ascontiguousarray(d, dtype=np.float64) for d in b.data]
+        D = ctypes.POINTER(ctypes.c_double)
+        xs = (D * n)(*[x.ctypes.data_as(D) for x in self._xs])
+        nx = (ctypes.c_int * n)(*[x.size for x in self._xs])
+        ds = (ctypes.c_void_p * n)(*[d.ctypes.data for d in self._ds])
+        grp = None if group is None else (ctypes.c_int * n)(*[int(g) for g in group])
+        self._check(self.api.batch_capture(self.h, xs, nx, ds, grp), "batch_capture")
+        for c in b.ctxs:  # the capture rewrote the contexts' histories
+            c._touch()
+
+    def launch(self):
+        self._check(self.api.batch_launch(self.h, None), "batch_launch")
+
+    def results(self):
+        import ctypes
+
+        n = len(self.batch.ctxs)
+        J = np.zeros(n)
+        dJ = [np.zeros(x.size) for x in self._xs]
+        D = ctypes.POINTER(ctypes.c_double)
+        arr = (D * n)(*[g.ctypes.data_as(D) for g in dJ])
+        self._check(self.api.batch_results(self.h, None, J.ctypes.data_as(D), arr),
+                    "batch_results")
+        return [(float(J[i]), dJ[i]) for i in range(n)]
+
+    def evaluate(self):
+        """All problems once through the graph; returns (wall seconds, [(J, dJ)])."""
+        t0 = time.perf_counter()
+        self.launch()
+        res = self.results()
+        return time.perf_counter() - t0, res
+
+    def close(self):
+        if self.h:
+            self.api.batch_destroy(self.h)
+            self.h = None
+
+
+def groupings(problems) -> dict:
+    """Candidate branch groupings of the graph: all problems as parallel branches; the largest
+    grids first (on their own), then the rest in parallel; one group per grid size, largest
+    first; two interleaved halves by decreasing size."""
+    n = len(problems)
+    sizes = sorted({p.n for p in problems}, reverse=True)
+    order = longest_first(problems)
+    halves = [0] * n
+    for k, i in enumerate(order):
+        halves[i] = k % 2
+    return {"parallel": [0] * n,
+            "largest_first": [0 if p.n == sizes[0] else 1 for p in problems],
+            "by_size": [sizes.index(p.n) for p in problems],
+            "two_waves": halves}
+
+
+def autotune_graph(problems, nt_probe: int = 10, cache: str = CACHE, force: bool = False) -> dict:
+    """Chooses the launch geometry of the small grids and the branch grouping of the one-graph
+    batch by timing each candidate graph on a shortened copy of the batch (nt_probe steps);
+    caches the choice per batch signature."""
+    sig = "graph:" + signature(problems)
+    table = json.load(open(cache)) if os.path.exists(cache) else {}
+    if sig in table and not force:
+        return table[sig]
+    import dataclasses
+
+    probe = [dataclasses.replace(p, nt=nt_probe,
+                                 wl=dataclasses.replace(p.wl, nt=nt_probe)) for p in problems]
+    candidates = []
+    for small in ((8, 4), (2, 1)):
+        geometry = {"32": list(small), "64": list(small), "128": list(small), "256": [8, 4]}
+        batch = Batch(probe)
+        batch.set_geometry(geometry)
+        gb = None
+        for name, grp in groupings(probe).items():
+            if gb is None:
+                gb = GraphBatch(batch, grp)
+            else:
+                gb.capture(grp)
+            gb.evaluate()  # warm-up launch
+            t, _ = gb.evaluate()
+            candidates.append((t, name, geometry, grp))
+        gb.close()
+        batch.close()
+    t, name, geometry, grp = min(candidates, key=lambda c: c[0])
+    choice = {"grouping": name, "group": grp, "geometry": geometry, "probe_seconds": t,
+              "candidates": [[c[0], c[1], c[2]["64"]] for c in candidates]}
+    table[sig] = choice
+    os.makedirs(os.path.dirname(cache), exist_ok=True)
+    json.dump(table, open(cache, "w"), indent=1)
+    return choice
+
+
 def signature(problems) -> str:
     sizes = {}
     for p in problems:
@@ -205,22 +333,36 @@ def autotune(problems, nt_probe: int = 10, cache: str = CACHE, force: bool = Fal
 
 
 def run(nt: int = 100, repeats: int = 2):
+    """The batch three ways: one problem at a time (default geometry), host threads (autotuned
+    concurrency) and one CUDA graph (autotuned grouping), each the best of `repeats`; the
+    graph's results are checked against the ordinary evaluations of the same contexts."""
     problems = default_batch(nt)
+    gchoice = autotune_graph(problems)
     choice = autotune(problems)
+    n = len(problems)
     batch = Batch(problems)
     order = longest_first(problems)
-    # sequential: one problem at a time, default launch geometry
     batch.evaluate(1, order)
     t_seq = min(batch.evaluate(1, order)[0] for _ in range(repeats))
     batch.set_geometry(choice["geometry"])
     batch.evaluate(choice["concurrency"], order)
-    t_bat, res = min((batch.evaluate(choice["concurrency"], order) for _ in range(repeats)),
-                     key=lambda r: r[0])
+    t_thr = min(batch.evaluate(choice["concurrency"], order)[0] for _ in range(repeats))
+    batch.set_geometry(gchoice["geometry"])
+    gb = GraphBatch(batch, gchoice["group"])
+    gb.evaluate()
+    t_gr, res = min((gb.evaluate() for _ in range(repeats)), key=lambda r: r[0])
+    same = all(J == Jr and np.array_equal(g, gr)
+               for (J, g), (Jr, gr) in zip(res, gb.reference))
+    gb.close()
     batch.close()
-    n = len(problems)
-    return {"problems": signature(problems), "sequential_s": t_seq, "batched_s": t_bat,
-            "sequential_evals_per_s": n / t_seq, "batched_evals_per_s": n / t_bat,
-            "speedup": t_seq / t_bat, "schedule": choice}
+    return {"problems": signature(problems), "sequential_s": t_seq,
+            "sequential_evals_per_s": n / t_seq,
+            "graph_s": t_gr, "graph_evals_per_s": n / t_gr, "graph_speedup": t_seq / t_gr,
+            "graph_equals_single_problem_runs": same,
+            "threads_s": t_thr, "threads_evals_per_s": n / t_thr, "threads_speedup": t_seq / t_thr,
+            "graph_schedule": {k: gchoice[k] for k in ("grouping", "geometry", "probe_seconds",
+                                                       "candidates")},
+            "threads_schedule": choice}
 
 
 def run_distributed(nt: int = 100):

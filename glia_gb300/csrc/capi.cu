@@ -2,10 +2,13 @@
 // all exceptions, stores the message on the context and returns a status code.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
+#include <map>
 #include <memory>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "common.cuh"
 #include "engine.hpp"
@@ -284,6 +287,178 @@ int glia_get_timing(glia_ctx* ctx, int slot, const char** name, int64_t* launche
     count = e.timing(slot, name, launches, ms, algorithmic_bytes);
   });
   return rc == GLIA_OK ? count : rc;
+}
+
+}  // extern "C"
+
+// ---- batches of evaluations in one CUDA graph ------------------------------------------------
+struct glia_batch {
+  std::vector<glia_ctx*> ctxs;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t root = nullptr;
+  std::vector<cudaEvent_t> events;
+  std::string err;
+  ~glia_batch() { release(); }
+  void release() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
+    events.clear();
+  }
+  cudaEvent_t event() {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+      throw glia::Error(GLIA_ERR_CUDA, "cudaEventCreateWithFlags failed");
+    events.push_back(e);
+    return e;
+  }
+};
+
+namespace {
+
+#define BATCH_CUDA(call)                                                                  \
+  do {                                                                                    \
+    const cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess) throw glia::Error(GLIA_ERR_CUDA, std::string(#call) + ": " +     \
+                                                                cudaGetErrorString(e_));  \
+  } while (0)
+
+template <class F>
+int batch_guarded(glia_batch* b, F&& f) {
+  if (!b) return GLIA_ERR_INVALID;
+  try {
+    f();
+    return GLIA_OK;
+  } catch (const glia::Error& e) {
+    b->err = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    b->err = "host allocation failed";
+    return GLIA_ERR_OOM;
+  } catch (const std::exception& e) {
+    b->err = e.what();
+    return GLIA_ERR_INVALID;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int glia_batch_create(glia_ctx* const* ctxs, int n, glia_batch** out) {
+  if (!out) return GLIA_ERR_INVALID;
+  *out = nullptr;
+  if (!ctxs || n < 1) return GLIA_ERR_INVALID;
+  for (int i = 0; i < n; i++)
+    if (!ctxs[i] || !ctxs[i]->eng) return GLIA_ERR_INVALID;
+  glia_batch* b = new (std::nothrow) glia_batch();
+  if (!b) return GLIA_ERR_OOM;
+  b->ctxs.assign(ctxs, ctxs + n);
+  if (cudaStreamCreateWithFlags(&b->root, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete b;
+    return GLIA_ERR_CUDA;
+  }
+  *out = b;
+  return GLIA_OK;
+}
+
+int glia_batch_capture(glia_batch* b, const double* const* x, const int* nx,
+                       const void* const* d1, const int* group) {
+  if (!b || !x || !nx || !d1) return GLIA_ERR_INVALID;
+  return batch_guarded(b, [&] {
+    const int n = (int)b->ctxs.size();
+    b->release();
+    // host part of every evaluation (coefficients, Phi p, data), outside the capture
+    for (int i = 0; i < n; i++) {
+      glia_ctx* c = b->ctxs[i];
+      if (!x[i] || !d1[i]) throw glia::Error(GLIA_ERR_INVALID, "null x or d1");
+      if (!c->eng->stream())
+        throw glia::Error(GLIA_ERR_INVALID, "contexts of a batch need a non-default stream");
+      try {
+        c->eng->eval_prepare(x[i], nx[i], d1[i]);
+      } catch (const glia::Error& e) {
+        c->err = e.what();
+        throw glia::Error(e.code, "context " + std::to_string(i) + ": " + e.what());
+      }
+    }
+    std::map<int, std::vector<int>> groups;
+    for (int i = 0; i < n; i++) groups[group ? group[i] : 0].push_back(i);
+    BATCH_CUDA(cudaStreamBeginCapture(b->root, cudaStreamCaptureModeRelaxed));
+    cudaGraph_t graph = nullptr;
+    try {
+      cudaEvent_t start = b->event();
+      BATCH_CUDA(cudaEventRecord(start, b->root));
+      for (auto& kv : groups) {
+        for (int i : kv.second) {
+          glia_ctx* c = b->ctxs[i];
+          cudaStream_t s = static_cast<cudaStream_t>(c->eng->stream());
+          BATCH_CUDA(cudaStreamWaitEvent(s, start, 0));  // fork: the branch joins the capture
+          try {
+            c->eng->eval_capture();
+          } catch (const glia::Error& e) {
+            c->err = e.what();
+            throw glia::Error(e.code, "context " + std::to_string(i) + ": " + e.what());
+          }
+          cudaEvent_t done = b->event();
+          BATCH_CUDA(cudaEventRecord(done, s));
+          BATCH_CUDA(cudaStreamWaitEvent(b->root, done, 0));  // join
+        }
+        start = b->event();  // the next group starts when this one is done
+        BATCH_CUDA(cudaEventRecord(start, b->root));
+      }
+      BATCH_CUDA(cudaStreamEndCapture(b->root, &graph));
+    } catch (...) {
+      cudaGraph_t junk = nullptr;
+      cudaStreamEndCapture(b->root, &junk);
+      if (junk) cudaGraphDestroy(junk);
+      cudaGetLastError();
+      throw;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&b->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+      b->exec = nullptr;
+      throw glia::Error(GLIA_ERR_CUDA, std::string("cudaGraphInstantiate: ") +
+                                           cudaGetErrorString(ie));
+    }
+  });
+}
+
+int glia_batch_launch(glia_batch* b, void* stream) {
+  if (!b) return GLIA_ERR_INVALID;
+  return batch_guarded(b, [&] {
+    if (!b->exec) throw glia::Error(GLIA_ERR_STATE, "no captured batch graph");
+    BATCH_CUDA(cudaGraphLaunch(b->exec, stream ? static_cast<cudaStream_t>(stream) : b->root));
+  });
+}
+
+int glia_batch_results(glia_batch* b, void* stream, double* J, double* const* dJ) {
+  if (!b || !J) return GLIA_ERR_INVALID;
+  return batch_guarded(b, [&] {
+    BATCH_CUDA(cudaStreamSynchronize(stream ? static_cast<cudaStream_t>(stream) : b->root));
+    for (size_t i = 0; i < b->ctxs.size(); i++) {
+      glia_ctx* c = b->ctxs[i];
+      try {
+        c->eng->eval_finish(&J[i], dJ ? dJ[i] : nullptr);
+      } catch (const glia::Error& e) {
+        c->err = e.what();
+        throw glia::Error(e.code, "context " + std::to_string(i) + ": " + e.what());
+      }
+    }
+  });
+}
+
+const char* glia_batch_last_error(const glia_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+int glia_batch_destroy(glia_batch* b) {
+  if (!b) return GLIA_ERR_INVALID;
+  if (b->root) cudaStreamSynchronize(b->root);
+  b->release();
+  if (b->root) cudaStreamDestroy(b->root);
+  delete b;
+  cudaGetLastError();
+  return GLIA_OK;
 }
 
 }  // extern "C"

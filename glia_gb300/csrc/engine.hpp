@@ -45,6 +45,15 @@ class EngineBase {
   virtual void get_state(int i, void* out) = 0;
   virtual void get_adjoint(int i, void* out) = 0;
   virtual void evaluate(const double* x, int nx, const void* d1, double* J, double* dJ) = 0;
+  // An evaluation split for CUDA-graph capture (batches): eval_prepare does the host-dependent
+  // part for x and d1 (coefficients, Phi p, data upload); eval_capture enqueues the forward,
+  // residual, adjoint and gradient sweeps on the context's stream while that stream is being
+  // captured, with no host synchronisation; eval_finish reads the results after the captured
+  // graph has run.
+  virtual void eval_prepare(const double* x, int nx, const void* d1) = 0;
+  virtual void eval_capture() = 0;
+  virtual void eval_finish(double* J, double* dJ) = 0;
+  virtual void* stream() const = 0;
   virtual glia_stats stats() const = 0;
   virtual void selftest_bounded_wait() = 0;
   virtual void reset_stats() = 0;

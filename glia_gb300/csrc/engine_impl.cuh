@@ -53,6 +53,7 @@ static __global__ void k_solve_config(DevScalars* s, double a_cn, double pc_c, d
 static __global__ void k_acc_reset(DevScalars* s) {
   for (int q = 0; q < 8; q++) s->acc[q] = 0.0;
 }
+static __global__ void k_keep_red0(DevScalars* s) { s->m1_keep = s->red[0]; }
 static __global__ void k_solve_stats_reset(DevScalars* s) {
   s->sum_its[0] = s->sum_its[1] = s->sum_its[2] = 0;
   s->nsolves = 0;
@@ -151,6 +152,7 @@ class Engine final : public EngineBase {
     if (hsc_) cudaFreeHost(hsc_);
     if (hst_) cudaFreeHost(hst_);
     if (own_stream_) cudaStreamDestroy(own_stream_);
+    if (cap_side_) cudaStreamDestroy(cap_side_);
   }
 
   // ------------------------------------------------------------------------------------------
@@ -344,7 +346,9 @@ class Engine final : public EngineBase {
     r2c(r2c1_, c, chat);
     d_front<false>(chat, nullptr);
     d_back<EPI_SETUP>(chat, cx, xhat_, rhat_, R(0));
-    if (use_graph()) {
+    if (capture_) {
+      capture_pcg_loop();  // the loop as a conditional node of the graph being captured
+    } else if (use_graph()) {
       GLIA_CUDA(cudaGraphLaunch(cg_exec_, stream_));  // the whole PCG loop, no host round trip
       graph_solves_ = true;
     } else {
@@ -432,14 +436,9 @@ class Engine final : public EngineBase {
   template <int NN, int EPI, bool IN2>
   void xfwd_n(const R* G, const R* aux_in, const R* cx, R* out, R* aux_out, R scale, int blocks) {
     if constexpr (std::is_same<R, float>::value) {
-      if constexpr (IN2) {
-        if (xfwd_direct_ && EPI != EPI_APPLYD)
-          k_xfwd_own<NN, EPI, true><<<blocks, 256, xfwd_own_smem_bytes<NN>(), stream_>>>(
-              g_, G, aux_in, cx, out, aux_out, scale, sc_, ws_, tw256_);
-        else
-          k_xfwd_own<NN, EPI><<<blocks, 256, xfwd_own_smem_bytes<NN>(), stream_>>>(
-              g_, G, aux_in, cx, out, aux_out, scale, sc_, ws_, tw256_);
-      }
+      if constexpr (IN2)
+        k_xfwd_own<NN, EPI><<<blocks, 256, xfwd_own_smem_bytes<NN>(), stream_>>>(
+            g_, G, aux_in, cx, out, aux_out, scale, sc_, ws_, tw256_);
       else
         k_xfwd<NN, EPI><<<blocks, 256, 0, stream_>>>(g_, G, aux_in, cx, out, aux_out, scale, sc_,
                                                      ws_, tw256_);
@@ -506,15 +505,9 @@ class Engine final : public EngineBase {
         xres_inv_ = sms_ * std::min(per_sm(k_xinv<NN, 0, true>, xinv_smem_bytes<NN, 0>()),
                                     per_sm(k_xinv<NN, 1, true>, xinv_smem_bytes<NN, 1>()));
         constexpr int fs = xfwd_own_smem_bytes<NN>();
-        // forward x pass: epilogue spectra staged through the slots, or read directly by the
-        // epilogue (GLIA_XFWD_DIRECT=1)
-        const char* xd = std::getenv("GLIA_XFWD_DIRECT");
-        xfwd_direct_ = xd && xd[0] == '1';
         xres_fwd_ = sms_ * std::min({per_sm(k_xfwd_own<NN, EPI_APPLYD>, fs),
                                      per_sm(k_xfwd_own<NN, EPI_SETUP>, fs),
-                                     per_sm(k_xfwd_own<NN, EPI_CGW>, fs),
-                                     per_sm(k_xfwd_own<NN, EPI_SETUP, true>, fs),
-                                     per_sm(k_xfwd_own<NN, EPI_CGW, true>, fs)});
+                                     per_sm(k_xfwd_own<NN, EPI_CGW>, fs)});
         // y-inverse rows staged by bulk copies (default) or per-thread cp.async
         // (GLIA_YINV_BULK=0)
         const char* yb = std::getenv("GLIA_YINV_BULK");
@@ -623,9 +616,70 @@ class Engine final : public EngineBase {
     if (g) cudaGraphDestroy(g);
   }
 
+  // Inside a capture of stream_: [k_cond_set] -> WHILE(cond) { iteration; k_cond_step }, the
+  // same loop as the per-engine PCG graph, added as nodes of the graph being captured (its body
+  // captured from a side stream into the conditional node's body graph).
+  void capture_pcg_loop() {
+    cudaStreamCaptureStatus cst;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    GLIA_CUDA(cudaStreamGetCaptureInfo(stream_, &cst, nullptr, &cg, &deps, nullptr, &nd));
+    if (cst != cudaStreamCaptureStatusActive)
+      throw Error(GLIA_ERR_STATE, "eval_capture: the context's stream is not being captured");
+    cudaGraphConditionalHandle h;
+    GLIA_CUDA(cudaGraphConditionalHandleCreate(&h, cg, 0, 0));
+    k_cond_set<<<1, 1, 0, stream_>>>(sc_, h);
+    GLIA_LAUNCH_CHECK();
+    GLIA_CUDA(cudaStreamGetCaptureInfo(stream_, &cst, nullptr, &cg, &deps, nullptr, &nd));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t loop;
+    GLIA_CUDA(cudaGraphAddNode(&loop, cg, deps, nullptr, nd, &cp));
+    GLIA_CUDA(cudaStreamUpdateCaptureDependencies(stream_, &loop, nullptr, 1,
+                                                  cudaStreamSetCaptureDependencies));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if (!cap_side_) GLIA_CUDA(cudaStreamCreateWithFlags(&cap_side_, cudaStreamNonBlocking));
+    cudaStream_t saved = stream_;
+    stream_ = cap_side_;
+    set_plan_streams(cap_side_);
+    bool capturing = false;
+    try {
+      GLIA_CUDA(cudaStreamBeginCaptureToGraph(cap_side_, body, nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeRelaxed));
+      capturing = true;
+      cg_iteration();
+      k_cond_step<<<1, 1, 0, cap_side_>>>(sc_, h);
+      GLIA_LAUNCH_CHECK();
+      cudaGraph_t captured = nullptr;
+      capturing = false;
+      GLIA_CUDA(cudaStreamEndCapture(cap_side_, &captured));
+    } catch (...) {
+      if (capturing) {
+        cudaGraph_t junk = nullptr;
+        cudaStreamEndCapture(cap_side_, &junk);
+      }
+      stream_ = saved;
+      set_plan_streams(saved);
+      throw;
+    }
+    stream_ = saved;
+    set_plan_streams(saved);
+    cap_solves_ += 1;
+  }
+  void set_plan_streams(cudaStream_t s) {
+    for (cufftHandle p : {r2c1_, c2r1_, r2c3_, c2r3_}) GLIA_CUFFT(cufftSetStream(p, s));
+    if (zpass_) GLIA_CUFFT(cufftSetStream(p2d_, s));
+    if (xpass_ && !own_)
+      for (cufftHandle p : {r2c2d3_, c2r2d3_}) GLIA_CUFFT(cufftSetStream(p, s));
+  }
+
   // Reads the device-side solve statistics of the sweep and reports the first failed solve.
   void sync_sweep() {
-    if (ref_) return;
+    if (ref_ || capture_) return;  // a captured evaluation reads its statistics in eval_finish
     GLIA_CUDA(cudaMemcpyAsync(hsc_, sc_, sizeof(DevScalars), cudaMemcpyDeviceToHost, stream_));
     GLIA_CUDA(cudaStreamSynchronize(stream_));
     tm_.harvest();
@@ -1648,7 +1702,7 @@ class Engine final : public EngineBase {
     const bool want_grad = dJ != nullptr;
     if (J) st_.nb_obj_evals++;
     if (want_grad) st_.nb_grad_evals++;
-    const int np = opt_.np, nk = opt_.nk, nr = opt_.nr;
+    const int np = opt_.np;
     if (want_grad) std::fill(dJ, dJ + nx(), 0.0);
     R* data = d1_buf();
     import_field(d1, data);
@@ -1696,6 +1750,11 @@ class Engine final : public EngineBase {
       GLIA_CUDA(cudaStreamSynchronize(stream_));
       std::memcpy(acc, hsc_->acc, sizeof(acc));
     }
+    coefficient_gradient(acc, dJ, h3);
+  }
+  // kappa and rho blocks of the gradient from the time integrals acc (DevScalars::acc)
+  void coefficient_gradient(const double* acc, double* dJ, double h3) {
+    const int np = opt_.np, nk = opt_.nk, nr = opt_.nr;
     if (update_kappa()) {
       double Twm, Tgm, Tcsf;
       if (!ref_ && kappa_used_trick_) {
@@ -1719,6 +1778,111 @@ class Engine final : public EngineBase {
       if (nr > 2) dJ[np + nk + 2] = acc[5] * h3;
     }
   }
+  // ---- evaluation captured into a CUDA graph (glia_batch_*) -------------------------------
+  // The fused engine's evaluate() with every host read moved to eval_finish: the coefficient
+  // update, Phi p and the data upload run before the capture (they depend on x on the host), the
+  // sweeps are captured with their PCG loops as conditional nodes, and J, the kappa / rho time
+  // integrals, the Phi^T product and the solve statistics stay on the device until eval_finish.
+  // One-snapshot objective, on-the-fly Phi (phi_store = 0), the reference default.
+  void eval_prepare(const double* x, int nxin, const void* d1) override {
+    if (ref_) throw Error(GLIA_ERR_INVALID, "graph-captured evaluations need the fused engine");
+    if (two_tp_ || opt_.phi_store)
+      throw Error(GLIA_ERR_INVALID,
+                  "graph-captured evaluations support one snapshot and phi_store = 0");
+    if (hist_mode_ == GLIA_HISTORY_OFF)
+      throw Error(GLIA_ERR_STATE, "graph-captured evaluations need a time history");
+    if (tm_.on) throw Error(GLIA_ERR_STATE, "disable timing before capturing an evaluation");
+    if (nxin != nx())
+      throw Error(GLIA_ERR_INVALID, "x has " + std::to_string(nxin) + " entries, expected " +
+                                        std::to_string(nx()));
+    cap_x_.assign(x, x + nxin);
+    import_field(d1, d1_buf());
+    update_coefficients(x);
+    if (apply_phi()) phi_apply_into(c0_, x);
+    const double h = 2.0 * M_PI / g_.n, h3 = h * h * h;
+    cap_reg_ = 0;
+    if (opt_.regularization_norm == 0) {
+      if (opt_.beta != 0) cap_reg_ = vdot_any(c0_, c0_) * 0.5 * opt_.beta * h3;
+    } else {
+      for (int i = 0; i < opt_.np; i++) cap_reg_ += x[i] * x[i];
+      cap_reg_ *= 0.5 * opt_.beta;
+    }
+    ensure_history();
+    // buffers the sweeps allocate on first use, allocated now (never while capturing)
+    if (!full()) {
+      pnt();
+      cfin();
+      tmp2();
+    }
+    if (!kappa_trick_ok()) ga3();
+    GLIA_CUDA(cudaStreamSynchronize(stream_));
+    cap_ready_ = true;
+  }
+  void eval_capture() override {
+    if (!cap_ready_) throw Error(GLIA_ERR_STATE, "eval_capture needs eval_prepare first");
+    const glia_stats saved = st_;  // capturing runs nothing: the counts come with eval_finish
+    capture_ = true;
+    cap_solves_ = 0;
+    try {
+      k_solve_stats_reset<<<1, 1, 0, stream_>>>(sc_);
+      GLIA_LAUNCH_CHECK();
+      solve_state_internal();
+      k_obs_residual<R><<<red_blocks_, kThreads, 0, stream_>>>(N_, ct_, obs_, d1_buf(), pt_,
+                                                               sc_, ws_);
+      GLIA_LAUNCH_CHECK();
+      k_keep_red0<<<1, 1, 0, stream_>>>(sc_);
+      GLIA_LAUNCH_CHECK();
+      solve_adjoint_internal(true);
+      if (apply_phi()) {  // p gradient: Phi^T (alpha_0 - beta c_0), scaled in eval_finish
+        if (opt_.beta != 0) vaxpy_any(p0_, -opt_.beta, c0_);
+        k_phi_applyT<R><<<phi_np_, kThreads, 0, stream_>>>(g_, phi_boxes_, phi_store_, p0_,
+                                                            phi_p_);
+        GLIA_LAUNCH_CHECK();
+      }
+    } catch (...) {
+      capture_ = false;
+      st_ = saved;
+      throw;
+    }
+    capture_ = false;
+    cap_total_solves_ = st_.total_diffusion_solves - saved.total_diffusion_solves;
+    st_ = saved;
+  }
+  void eval_finish(double* J, double* dJ) override {
+    if (!cap_ready_) throw Error(GLIA_ERR_STATE, "eval_finish needs a captured evaluation");
+    std::vector<double> pp(std::max(phi_np_, 1));
+    GLIA_CUDA(cudaMemcpyAsync(hsc_, sc_, sizeof(DevScalars), cudaMemcpyDeviceToHost, stream_));
+    if (apply_phi())
+      GLIA_CUDA(cudaMemcpyAsync(pp.data(), phi_p_, phi_np_ * sizeof(double),
+                                cudaMemcpyDeviceToHost, stream_));
+    GLIA_CUDA(cudaStreamSynchronize(stream_));
+    const DevScalars& h = *hsc_;
+    st_.nb_obj_evals++;
+    st_.nb_grad_evals++;
+    st_.nb_state_solves++;
+    st_.nb_adjoint_solves++;
+    st_.diff_ksp_itr_state = h.sum_its[0];
+    st_.diff_ksp_itr_adj = h.sum_its[1];
+    st_.total_diffusion_solves += cap_total_solves_;
+    st_.total_pcg_iterations += h.sum_its[0] + h.sum_its[1] + h.sum_its[2];
+    st_.max_ksp_itr = std::max(st_.max_ksp_itr, h.max_its);
+    st_.last_rnorm = h.last_dp;
+    st_.last_ksp_itr = h.it;
+    ksp_itr_ = h.it;
+    if (h.dev_fault) raise_device_fault();
+    if (h.err_status < 0) finish_solve(SolveStatus{h.err_status, h.err_its, h.last_dp});
+    const double hh = 2.0 * M_PI / g_.n, h3 = hh * hh * hh;
+    if (J) *J = h3 * 0.5 * h.m1_keep + cap_reg_;
+    if (!dJ) return;
+    std::fill(dJ, dJ + nx(), 0.0);
+    if (apply_phi()) {
+      const double s = 1.0 / phi_max_all();
+      for (int i = 0; i < opt_.np; i++) dJ[i] = -h3 * pp[i] * s;
+    }
+    coefficient_gradient(h.acc, dJ, h3);
+  }
+  void* stream() const override { return stream_; }
+
   // p gradient (src/grad/DerivativeOperatorsRD.cpp:164-187)
   void p_gradient(const double* x, double* dJ, double h3) {
     const int np = opt_.np;
@@ -2089,7 +2253,12 @@ class Engine final : public EngineBase {
   bool zpass2_ = true;               // z pass with two real lines per complex transform
   bool yinv_bulk_ = true;            // y-inverse rows staged by bulk copies
   bool own_ = false;  // own y and z passes (x pass on): no cuFFT inside the D apply
-  bool xfwd_direct_ = false;  // k_xfwd_own epilogue reads its spectra from global memory
+  // graph-captured evaluations (eval_prepare / eval_capture / eval_finish)
+  bool capture_ = false, cap_ready_ = false;
+  cudaStream_t cap_side_ = nullptr;  // captures the PCG loop bodies
+  int64_t cap_solves_ = 0, cap_total_solves_ = 0;
+  double cap_reg_ = 0;
+  std::vector<double> cap_x_;
   float2* tw_ = nullptr;
   char* fft_ws_ = nullptr;
   char* batch_ws_ = nullptr;

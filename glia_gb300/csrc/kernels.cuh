@@ -41,6 +41,7 @@ struct DevScalars {
   double last_dp;
   int dev_fault;         // a bounded device wait ran out (1: TMA copy did not arrive)
   int pad2;
+  double m1_keep;        // ||O c(1) - d||^2 of a graph-captured evaluation (read after it ran)
 };
 
 __device__ __forceinline__ int conv_test(double rn, const DevScalars* s) {

@@ -456,10 +456,8 @@ constexpr int xfwd_own_smem_bytes() {
 // divergence i w_x F_x M_x + F_x M_r, epilogue of k_spec_div. The CTA's inputs form a stream of
 // items (M_x, M_r and the epilogue's spectra of its first tile, then of the next, ...) through
 // two shared-memory slots: item i sits in slot i % 2 and, once consumed, its slot receives item
-// i + 2 (cp.async). DIRECT: the epilogue's spectra are read from global memory by the epilogue
-// itself (each warp reads two 128-byte row segments per element, as it writes them), so the slots
-// carry only M_x and M_r and the next tile's pair is always in flight behind the current one.
-template <int NN, int EPI, bool DIRECT = false>
+// i + 2 (cp.async).
+template <int NN, int EPI>
 __global__ void __launch_bounds__(256, 2)
     k_xfwd_own(Geo g, const float* __restrict__ M2, const float* __restrict__ aux_in,
                const float* __restrict__ cx, float* __restrict__ out, float* __restrict__ aux_out,
@@ -487,7 +485,7 @@ __global__ void __launch_bounds__(256, 2)
   float2* O = reinterpret_cast<float2*>(out);
   float2* AO = reinterpret_cast<float2*>(aux_out);
   const int naux = EPI == EPI_APPLYD ? 0 : (EPI == EPI_SETUP && CX ? 2 : 1);
-  const int NI = DIRECT ? 2 : 2 + naux;
+  const int NI = 2 + naux;
   const int mytiles =
       (int)blockIdx.x < ntiles ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
                                : 0;
@@ -533,13 +531,11 @@ __global__ void __launch_bounds__(256, 2)
             dsum[m2][k2].y += y.y;
           });
     }
-    if (!DIRECT) {
-      if (naux == 2)
-        cp_async_wait<0>();
-      else
-        cp_async_wait<1>();
-      __syncthreads();
-    }
+    if (naux == 2)
+      cp_async_wait<0>();
+    else
+      cp_async_wait<1>();
+    __syncthreads();
     const float2* SA = slot(i0 + 2);
     const float2* SX = slot(i0 + 3);
 #pragma unroll
@@ -548,20 +544,13 @@ __global__ void __launch_bounds__(256, 2)
 #pragma unroll
       for (int k2 = 0; k2 < R2; k2++) {
         const int kx = k1 + R1 * k2;
-        const int idx = kx * plane + col.q;
-        float2 av = make_float2(0.f, 0.f), xv = make_float2(0.f, 0.f);
-        if (DIRECT) {
-          if (naux) av = AX[idx];
-          if (naux == 2) xv = CX[idx];
-        } else {
-          if (naux) av = SA[kx * T + c];
-          if (naux == 2) xv = SX[kx * T + c];
-        }
-        xfwd_epilogue<NN, EPI>(dsum[m2][k2], kx, idx, col, a, pcc, invN, scale, av, xv, naux == 2,
-                               O, AO, acc);
+        const float2 av = naux ? SA[kx * T + c] : make_float2(0.f, 0.f);
+        const float2 xv = naux == 2 ? SX[kx * T + c] : make_float2(0.f, 0.f);
+        xfwd_epilogue<NN, EPI>(dsum[m2][k2], kx, kx * plane + col.q, col, a, pcc, invN, scale, av,
+                               xv, naux == 2, O, AO, acc);
       }
     }
-    if (!DIRECT && naux) {
+    if (naux) {
       __syncthreads();  // the epilogue's slots are read: stage the next tile's M_x (and M_r)
       issue(i0 + 4);
       if (naux == 2) issue(i0 + 5);

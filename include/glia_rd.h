@@ -241,6 +241,32 @@ int glia_set_timing(glia_ctx* ctx, int enable);
 int glia_get_timing(glia_ctx* ctx, int slot, const char** name, int64_t* launches, double* ms,
                     double* algorithmic_bytes);
 
+/* ---- batches of gradient evaluations in one CUDA graph ---------------------------------------
+ * The batched form of DerivativeOperatorsRD::evaluateObjectiveAndGradient
+ * (src/grad/DerivativeOperatorsRD.cpp:130-226) over independent problems, one context each (the
+ * reference has no batch interface: it evaluates one problem per process). glia_batch_capture
+ * runs the host part of every evaluation at its x and d1 (coefficient update, Phi p, data in the
+ * contexts' pointer modes), then captures all evaluations into one graph: a fork from the
+ * batch's stream into every context's stream, each context's forward, adjoint and gradient
+ * sweeps with its PCG loops as conditional WHILE nodes, a join. group[i] (NULL: all 0) orders
+ * the branches: contexts of one group run as parallel branches, groups one after another in
+ * increasing order. glia_batch_launch launches the graph once (stream NULL = the batch's own
+ * stream); every launch recomputes the evaluations captured at those x and d1 (data can be
+ * changed in place between launches; a new x needs a new capture). glia_batch_results waits for
+ * the launch and writes J[i] and dJ[i] (np + nk + nr entries each; dJ NULL: objectives only).
+ * Requirements: the fused engine, one snapshot, phi_store = 0, a history mode other than OFF,
+ * timing disabled, every context on its own non-default stream, and one ordinary evaluation of
+ * each context beforehand (its first call sets up the plans and graphs a capture cannot
+ * create). Errors name the failing context; its own message is in glia_last_error. */
+typedef struct glia_batch glia_batch;
+int glia_batch_create(glia_ctx* const* ctxs, int n, glia_batch** out);
+int glia_batch_capture(glia_batch* b, const double* const* x, const int* nx,
+                       const void* const* d1, const int* group);
+int glia_batch_launch(glia_batch* b, void* stream);
+int glia_batch_results(glia_batch* b, void* stream, double* J, double* const* dJ);
+const char* glia_batch_last_error(const glia_batch* b);
+int glia_batch_destroy(glia_batch* b);
+
 /* ---- data mismatch without allocation (extension; no counterpart in the reference) ---------
  * For callers that cannot let a library allocate device memory: code that captures its loss
  * evaluation into a CUDA graph (cudaMalloc is not allowed during stream capture), processes

@@ -38,7 +38,8 @@ def load() -> _abi.Bound:
         lib = ctypes.CDLL(LIB)
         _api = _abi.Bound(lib, "oracle_glia_", optional=("set_timing", "get_timing", "mismatch_f32_noalloc",
                                                        "set_launch_geometry",
-                                                       "selftest_bounded_wait"))
+                                                       "selftest_bounded_wait",
+                                                       *_abi.BATCH_NAMES))
         for name, res, args in (
             ("oracle_fft_r2c", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
             ("oracle_fft_c2r", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),

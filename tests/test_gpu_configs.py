@@ -115,3 +115,60 @@ def test_gradient_256_matches_the_oracle_fixture(prec, tol):
     assert abs(J - want["J"]) <= tol * abs(want["J"])
     errs = _grad_errors(dJ, want["dJ"])
     assert max(errs) <= tol, errs
+
+
+def _data256(g, wl):
+    """The oracle's observation when the fixture exists, else this FP64 path's own forward with
+    the perturbed parameters, thresholded at 0.5."""
+    if os.path.exists(os.path.join(GOLDEN, "workload256_data.npz")):
+        from tests.golden.make_config1 import load_data
+
+        return load_data(256), "oracle fixture"
+    g.set_coefficients(k=wl.kappa * 0.8, rho=wl.rho * 1.2, k_gm_wm=wl.k_gm_wm)
+    c1 = g.solve_state(g.phi_apply(wl.p_obs()))
+    g.set_coefficients(k=wl.kappa, rho=wl.rho, k_gm_wm=wl.k_gm_wm)
+    return (c1 > 0.5).astype(np.float64), "FP64 GPU forward"
+
+
+@pytest.mark.skipif(os.environ.get("GLIA_SLOW") != "1",
+                    reason="opt-in (GLIA_SLOW=1): 16 FP64 objective evaluations at 256^3, ~7 min")
+def test_gradient_256_central_differences():
+    """DerivativeOperators::checkGradient's protocol (src/grad/DerivativeOperators.cpp:369-450)
+    on the 256^3 workload: central differences (h = 1e-3) of J along 8 random unit directions
+    (seed 3) against the adjoint gradient, FP64 fused path, PCG rtol 1e-10 so that the PCG
+    tolerance stays below the difference quotient's resolution. The p block is the exact
+    discrete adjoint; kappa and rho are the reference's trapezoid quadratures."""
+    import json
+    import time
+
+    wl = syn.GradientWorkload(n=256, nt=100)
+    tissue = wl.tissue()
+    centers = wl.centers(tissue)
+    g = gpu(256, FP64)
+    syn.setup_context(g, wl, tissue, centers, _abi.GLIA_HISTORY_CHECKPOINT, 10)
+    g.set_obs_filter(np.ones(256 ** 3))
+    g.set_pcg(1e-10, 5000)
+    d1, source = _data256(g, wl)
+    x = wl.x_eval()
+    t0 = time.time()
+    J, grad = g.eval_objective_and_gradient(x, d1)
+    rng = np.random.default_rng(3)
+    h, np_ = 1e-3, wl.n_gauss
+    rows = []
+    for _ in range(8):
+        d = rng.standard_normal(x.size)
+        d /= np.linalg.norm(d)
+        fd = (g.eval_objective(x + h * d, d1) - g.eval_objective(x - h * d, d1)) / (2 * h)
+        ad = float(grad @ d)
+        rows.append({"fd": fd, "adjoint": ad, "rel_err": abs(fd - ad) / abs(fd),
+                     "p_part": float(grad[:np_] @ d[:np_]),
+                     "kappa_part": float(grad[np_] * d[np_]),
+                     "rho_part": float(grad[np_ + 1] * d[np_ + 1])})
+    out = {"J": J, "data": source, "h": h, "rtol": 1e-10, "seconds": time.time() - t0,
+           "directions": rows, "max_rel_err": max(r["rel_err"] for r in rows)}
+    path = os.environ.get("GLIA_FD_OUT")
+    if path:
+        with open(path, "w") as f:
+            json.dump(out, f, indent=1)
+    print(json.dumps(out))
+    assert out["max_rel_err"] <= 1e-2
