@@ -1025,7 +1025,94 @@ class Engine final : public EngineBase {
                               cudaMemcpyHostToDevice, stream_));
     GLIA_CUDA(cudaMemcpyAsync(phi_centers_, centers, 3 * np * sizeof(double),
                               cudaMemcpyHostToDevice, stream_));
-    // Phi::setValues (stored mode, src/mat/Phi.cpp:96-130), B functions per batch
+    // Phi::setValues (stored mode, src/mat/Phi.cpp:96-130)
+    phi_max_each_.assign(np, 0.0);
+    const double sig_s = smoothing_factor * 2.0 * M_PI / g_.n;
+    const int Rh = sig_s > 0 ? (int)std::ceil(9.6 * sig_s / h) : 0;
+    if (2 * Rh + 1 <= g_.n) {
+      phi_values_on_boxes(boxes, sigma, sig_s, Rh);
+    } else {
+      phi_values_full_grid(boxes, sigma, smoothing_factor);
+    }
+    build_phi_cells(boxes);
+  }
+  // The smoother's 1-D taps w(d) / sum w for offsets d = -Rh ... Rh (sigma_s = 0: no smoothing,
+  // as weierstrassSmoother returns its input) and the four box passes of k_phi_box per batch of
+  // boxes (two scratch buffers of at most 16 M doubles each, or one box's region).
+  void phi_values_on_boxes(const std::vector<PhiBox>& boxes, double sigma, double sig_s, int Rh) {
+    const int np = (int)boxes.size(), n = g_.n;
+    const double h = 2.0 * M_PI / n, twopi = 2.0 * M_PI;
+    std::vector<double> taps(2 * Rh + 1, 1.0);
+    if (Rh > 0) {
+      auto w1 = [&](int i) {
+        const double a = i * h, b = i * h - twopi;
+        return std::exp((-a * a) / sig_s / sig_s / 2.0) + std::exp((-b * b) / sig_s / sig_s / 2.0);
+      };
+      double s1 = 0.0;
+      for (int i = 0; i < n; i++) s1 += w1(i);
+      for (int d = -Rh; d <= Rh; d++) taps[d + Rh] = w1(((d % n) + n) % n) / s1;
+    }
+    double* dtaps = dalloc<double>((int64_t)taps.size());
+    GLIA_CUDA(cudaMemcpyAsync(dtaps, taps.data(), taps.size() * sizeof(double),
+                              cudaMemcpyHostToDevice, stream_));
+    auto region = [&](const PhiBox& b) {
+      return (int64_t)(b.ext[0] + 2 * Rh) * (b.ext[1] + 2 * Rh) * (b.ext[2] + 2 * Rh);
+    };
+    constexpr int64_t kScratch = int64_t(16) << 20;
+    int64_t most = 1;
+    for (const PhiBox& b : boxes) most = std::max(most, region(b));
+    const int64_t cap = std::max(kScratch, most);
+    double* A = dalloc<double>(cap);
+    double* Bf = dalloc<double>(cap);
+    int64_t* doff = dalloc<int64_t>(np);
+    constexpr int xb = 16;
+    double* bmax = dalloc<double>((int64_t)np * xb);
+    std::vector<int64_t> off(np);
+    std::vector<double> hmax((size_t)np * xb);
+    for (int b0 = 0; b0 < np;) {
+      int nb = 0;
+      int64_t used = 0;
+      while (b0 + nb < np && (nb == 0 || used + region(boxes[b0 + nb]) <= cap)) {
+        off[b0 + nb] = used;
+        used += region(boxes[b0 + nb]);
+        nb++;
+      }
+      GLIA_CUDA(cudaMemcpyAsync(doff + b0, off.data() + b0, nb * sizeof(int64_t),
+                                cudaMemcpyHostToDevice, stream_));
+      const dim3 grid(xb, nb);
+      const PhiBox* bx = phi_boxes_ + b0;
+      const double* cc = phi_centers_ + 3 * b0;
+      k_phi_box<R, 0><<<grid, kThreads, 0, stream_>>>(g_, nb, bx, cc, sigma, Rh, dtaps, filter_,
+                                                       doff + b0, nullptr, A, phi_store_, nullptr);
+      GLIA_LAUNCH_CHECK();
+      k_phi_box<R, 1><<<grid, kThreads, 0, stream_>>>(g_, nb, bx, cc, sigma, Rh, dtaps, filter_,
+                                                       doff + b0, A, Bf, phi_store_, nullptr);
+      GLIA_LAUNCH_CHECK();
+      k_phi_box<R, 2><<<grid, kThreads, 0, stream_>>>(g_, nb, bx, cc, sigma, Rh, dtaps, filter_,
+                                                       doff + b0, Bf, A, phi_store_, nullptr);
+      GLIA_LAUNCH_CHECK();
+      k_phi_box<R, 3><<<grid, kThreads, 0, stream_>>>(g_, nb, bx, cc, sigma, Rh, dtaps, filter_,
+                                                       doff + b0, A, nullptr, phi_store_,
+                                                       bmax + (int64_t)b0 * xb);
+      GLIA_LAUNCH_CHECK();
+      b0 += nb;
+    }
+    GLIA_CUDA(cudaMemcpyAsync(hmax.data(), bmax, hmax.size() * sizeof(double),
+                              cudaMemcpyDeviceToHost, stream_));
+    GLIA_CUDA(cudaStreamSynchronize(stream_));
+    for (int b = 0; b < np; b++) {
+      double m = 0.0;
+      for (int q = 0; q < xb; q++) m = std::max(m, hmax[(size_t)b * xb + q]);
+      phi_max_each_[b] = m;
+    }
+    for (void* p : {(void*)dtaps, (void*)A, (void*)Bf, (void*)doff, (void*)bmax}) dfree(p);
+  }
+  // The same values through full-grid transforms (a smoother wider than the grid), B functions
+  // per batch: Phi::initialize on the grid, the smoother as a spectral multiplier, then
+  // truncation and extraction of each box.
+  void phi_values_full_grid(const std::vector<PhiBox>& boxes, double sigma,
+                            double smoothing_factor) {
+    const int np = (int)boxes.size();
     const int B = std::min(np, 8);
     ensure_batch_plans(B);
     R* full = dalloc<R>((int64_t)B * N_);
@@ -1035,7 +1122,6 @@ class Engine final : public EngineBase {
     double* bmax = dalloc<double>((int64_t)B * xb);
     std::vector<double> hmax((size_t)B * xb);
     const R* K = smoother_kernel(smoothing_factor * 2.0 * M_PI / g_.n);
-    phi_max_each_.assign(np, 0.0);
     for (int b0 = 0; b0 < np; b0 += B) {
       const int nb = std::min(B, np - b0);
       k_phi_gauss<R><<<pw_blocks_, kThreads, 0, stream_>>>(g_, nb, phi_centers_ + 3 * b0, sigma,
@@ -1063,7 +1149,10 @@ class Engine final : public EngineBase {
     dfree(fsp);
     dfree(bmax);
     destroy_batch_plans();
-    // cell lists for the gathered apply
+  }
+  // cell lists of the gathered apply
+  void build_phi_cells(const std::vector<PhiBox>& boxes) {
+    const int np = (int)boxes.size();
     const int cpd = (g_.n + 7) / 8;
     std::vector<std::vector<int>> lists((size_t)cpd * cpd * cpd);
     for (int i = 0; i < np; i++) {
@@ -1875,9 +1964,12 @@ class Engine final : public EngineBase {
     if (J) *J = h3 * 0.5 * h.m1_keep + cap_reg_;
     if (!dJ) return;
     std::fill(dJ, dJ + nx(), 0.0);
-    if (apply_phi()) {
+    if (apply_phi()) {  // the same products, in the same order, as p_gradient
       const double s = 1.0 / phi_max_all();
-      for (int i = 0; i < opt_.np; i++) dJ[i] = -h3 * pp[i] * s;
+      for (int i = 0; i < opt_.np; i++) {
+        const double v = pp[i] * s;
+        dJ[i] = v * -h3;
+      }
     }
     coefficient_gradient(h.acc, dJ, h3);
   }

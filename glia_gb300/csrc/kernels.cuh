@@ -775,6 +775,83 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// Phi::setValues on the compact boxes only. The smoother's periodised Gaussian (eight images,
+// unit sum) is the product of three 1-D kernels w(d) = exp(-(dh)^2 / 2s^2) + exp(-(dh - 2pi)^2 /
+// 2s^2) (d = offset mod n) over their sum, so W * f is three 1-D convolutions; w is cut at
+// |d| <= Rh voxels, where it is below 1e-20 of its peak. Four passes per batch of boxes (grid
+// (blocks per box, batch), one scratch region per box at scr_off[b]):
+//  0: f = exp(-(r / (sqrt 2 sigma))^2) filter on the box widened by Rh on each side (periodic
+//     grid indices, non-periodic distances, as Phi::initialize on the full grid);
+//  1, 2: convolution along z, then y, each narrowing that axis to the box;
+//  3: convolution along x, Phi::truncate (r / sigma <= 5), the box values into store, and the
+//     per-box maximum into boxmax[b * gridDim.x + blockIdx.x].
+// taps[d] multiplies the input at local index (output index + d), d = 0 ... 2 Rh (w is even).
+// Everything is FP64; store is R.
+template <typename R, int PASS>
+__global__ void __launch_bounds__(kThreads)
+    k_phi_box(Geo g, int batch, const PhiBox* __restrict__ boxes,
+              const double* __restrict__ centers, double sigma, int Rh,
+              const double* __restrict__ taps, const R* __restrict__ filter,
+              const int64_t* __restrict__ scr_off, const double* __restrict__ in,
+              double* __restrict__ out, R* __restrict__ store, double* __restrict__ boxmax) {
+  __shared__ double sh[kWarps];
+  const int b = blockIdx.y;
+  if (b >= batch) return;
+  const PhiBox B = boxes[b];
+  const int n = g.n, W = 2 * Rh + 1;
+  // extents of this pass's output: axes already convolved are box-sized, the others widened
+  const int ex = B.ext[0] + (PASS < 3 ? 2 * Rh : 0);
+  const int ey = B.ext[1] + (PASS < 2 ? 2 * Rh : 0);
+  const int ez = B.ext[2] + (PASS < 1 ? 2 * Rh : 0);
+  const int64_t cnt = (int64_t)ex * ey * ez;
+  const double h = 2.0 * 3.14159265358979323846 / n;
+  const double cx = centers[3 * b], cy = centers[3 * b + 1], cz = centers[3 * b + 2];
+  const double* src = PASS > 0 ? in + scr_off[b] : nullptr;
+  double* dst = PASS < 3 ? out + scr_off[b] : nullptr;
+  double m = 0.0;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cnt;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int ix = (int)(q / ((int64_t)ey * ez)), iy = (int)((q / ez) % ey), iz = (int)(q % ez);
+    if (PASS == 0) {
+      const int x = ((B.lo[0] - Rh + ix) % n + n) % n, y = ((B.lo[1] - Rh + iy) % n + n) % n,
+                z = ((B.lo[2] - Rh + iz) % n + n) % n;
+      const double dx = h * x - cx, dy = h * y - cy, dz = h * z - cz;
+      const double ratio = sqrt(dx * dx + dy * dy + dz * dz) / (sqrt(2.0) * sigma);
+      dst[q] = exp(-ratio * ratio) * (double)filter[((int64_t)x * n + y) * n + z];
+    } else if (PASS == 1) {  // input (ex, ey, ez + 2Rh)
+      const double* s = src + ((int64_t)ix * ey + iy) * (ez + 2 * Rh) + iz;
+      double v = 0.0;
+      for (int d = 0; d < W; d++) v += taps[d] * s[d];
+      dst[q] = v;
+    } else if (PASS == 2) {  // input (ex, ey + 2Rh, ez)
+      const double* s = src + ((int64_t)ix * (ey + 2 * Rh) + iy) * ez + iz;
+      double v = 0.0;
+      for (int d = 0; d < W; d++) v += taps[d] * s[(int64_t)d * ez];
+      dst[q] = v;
+    } else {  // input (ex + 2Rh, ey, ez); box output
+      const double* s = src + ((int64_t)ix * ey + iy) * ez + iz;
+      double v = 0.0;
+      for (int d = 0; d < W; d++) v += taps[d] * s[(int64_t)d * ey * ez];
+      const double dx = h * (B.lo[0] + ix) - cx, dy = h * (B.lo[1] + iy) - cy,
+                   dz = h * (B.lo[2] + iz) - cz;
+      const double r = sqrt(dx * dx + dy * dy + dz * dz);
+      const R rv = (r / sigma <= 5.0) ? (R)v : (R)0;
+      store[B.off + q] = rv;
+      m = fmax(m, (double)rv);
+    }
+  }
+  if (PASS == 3) {
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double bm = sh[0];
+      for (int w = 1; w < kWarps; w++) bm = fmax(bm, sh[w]);
+      boxmax[(int64_t)b * gridDim.x + blockIdx.x] = bm;
+    }
+  }
+}
+
 // Phi::apply: out = scale * sum_i p_i phi_i, gathered per output cell (cells of 8^3 voxels, box
 // lists in CSR order of increasing index), each output voxel written exactly once.
 template <typename R>

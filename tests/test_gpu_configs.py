@@ -171,4 +171,5 @@ def test_gradient_256_central_differences():
         with open(path, "w") as f:
             json.dump(out, f, indent=1)
     print(json.dumps(out))
-    assert out["max_rel_err"] <= 1e-2
+    # GB300, FP64, data of this path's own forward: worst direction 3.3e-5 (kappa dominates)
+    assert out["max_rel_err"] <= 1e-4
