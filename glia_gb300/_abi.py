@@ -112,6 +112,8 @@ SIGNATURES = {
     "set_phi": (c_int, [_CTX, _D, c_int, c_double, c_double]),
     "phi_apply": (c_int, [_CTX, _D, _P]),
     "phi_apply_transpose": (c_int, [_CTX, _P, _D]),
+    "phi_data_centers": (c_int, [_CTX, _P, c_double, c_double, c_double, c_double, c_int, _D,
+                                 POINTER(c_int), _P]),
     "set_obs_threshold": (c_int, [_CTX, _P, c_double]),
     "set_obs_filter": (c_int, [_CTX, _P]),
     "set_obs_threshold0": (c_int, [_CTX, _P, c_double]),

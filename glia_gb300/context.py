@@ -273,6 +273,27 @@ class Context:
             self._keep = []
         return pout
 
+    def phi_data_centers(self, data, sigma, data_threshold=0.05, gaussian_vol_frac=0.0,
+                         spacing_factor=2.0, with_frac=False):
+        """Phi::setGaussians(Vec data): (centres (np, 3), num_tumor_output field or None)."""
+        n, h = self.n, 2 * np.pi / self.n
+        space = spacing_factor * sigma / h
+        hits = [x for x in range(n) if space >= 1 and np.fmod(x, space) == 0.0]
+        cap = max(1, (len(range(hits[0], hits[-1] + 1, max(1, int(space)))) + 1) ** 3) \
+            if hits else 1
+        out = np.zeros(3 * cap, dtype=np.float64)
+        cnt = ctypes.c_int(0)
+        self._keep = []
+        try:
+            frac, pf = self._field_out(None) if with_frac else (None, None)
+            self._check(self.api.phi_data_centers(self._h, self._field_in(data), sigma,
+                                                  data_threshold, gaussian_vol_frac,
+                                                  spacing_factor, cap, _dptr(out),
+                                                  ctypes.byref(cnt), pf), "phi_data_centers")
+        finally:
+            self._keep = []
+        return out[:3 * cnt.value].reshape(-1, 3).copy(), frac
+
     def set_secondary_coefficients(self, k1, k2=0.0, k3=0.0):
         """DiffCoef::setSecondaryCoefficients: the diffusivity direction of solve_state(2)."""
         self._touch()

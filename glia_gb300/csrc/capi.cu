@@ -205,6 +205,16 @@ int glia_phi_apply(glia_ctx* ctx, const double* p, void* c0) {
   if (!p || !c0) return GLIA_ERR_INVALID;
   return guarded(ctx, [&](glia::EngineBase& e) { e.phi_apply(p, c0); });
 }
+int glia_phi_data_centers(glia_ctx* ctx, const void* data, double sigma, double data_threshold,
+                          double gaussian_vol_frac, double spacing_factor, int max_centers,
+                          double* centers, int* np_out, void* frac) {
+  if (!data || !np_out || (max_centers > 0 && !centers) || max_centers < 0)
+    return GLIA_ERR_INVALID;
+  return guarded(ctx, [&](glia::EngineBase& e) {
+    e.phi_data_centers(data, sigma, data_threshold, gaussian_vol_frac, spacing_factor,
+                       max_centers, centers, np_out, frac);
+  });
+}
 int glia_phi_apply_transpose(glia_ctx* ctx, const void* v, double* pout) {
   if (!v || !pout) return GLIA_ERR_INVALID;
   return guarded(ctx, [&](glia::EngineBase& e) { e.phi_apply_transpose(v, pout); });

@@ -32,6 +32,9 @@ class EngineBase {
   virtual void set_phi(const double* centers, int np, double sigma, double smoothing_factor) = 0;
   virtual void phi_apply(const double* p, void* c0) = 0;
   virtual void phi_apply_transpose(const void* v, double* pout) = 0;
+  virtual void phi_data_centers(const void* data, double sigma, double thr, double gvf,
+                                double spacing_factor, int max_centers, double* centers,
+                                int* np_out, void* frac) = 0;
   virtual void set_obs_threshold(const void* data, double thr) = 0;
   virtual void set_obs_filter(const void* f) = 0;
   virtual void set_obs_threshold0(const void* data, double thr) = 0;

@@ -1238,6 +1238,92 @@ class Engine final : public EngineBase {
     phi_applyT_from(tmp_, pout);
   }
 
+  // Phi::setGaussians(Vec data) (src/mat/Phi.cpp:615-1004) for one process: the ball and the
+  // lattice as the reference's loops make them (ball offsets over [(int)-r, (int)r] with
+  // |o| <= r; lattice from the first to the last fmod(X, space) == 0 index by X += space on an
+  // integer), counts by k_data_centers, selection count > gvf * interior in x-major order.
+  void phi_data_centers(const void* data, double sigma, double thr, double gvf,
+                        double spacing_factor, int max_centers, double* centers, int* np_out,
+                        void* frac) override {
+    const int n = g_.n;
+    const double h = 2.0 * M_PI / n, r = sigma / h, space = spacing_factor * sigma / h;
+    if (!(sigma > 0) || !(space >= 1.0) || !(gvf >= 0))
+      throw Error(GLIA_ERR_INVALID, "phi_data_centers: sigma > 0, gaussian_vol_frac >= 0 and a "
+                                    "centre spacing of at least one voxel are needed");
+    std::vector<int> offs;
+    const int lo = (int)(-r), hi = (int)r;
+    for (int i = lo; i <= hi; i++)
+      for (int j = lo; j <= hi; j++)
+        for (int k = lo; k <= hi; k++)
+          if (std::sqrt((double)(i * i + j * j + k * k)) <= r) {
+            offs.push_back(i);
+            offs.push_back(j);
+            offs.push_back(k);
+          }
+    const int interior = (int)offs.size() / 3;
+    std::vector<int> axis;
+    int first = -1, last = -1;
+    for (int x = 0; x < n; x++)
+      if (std::fmod((double)x, space) == 0.0) {
+        if (first < 0) first = x;
+        last = x;
+      }
+    for (int x = first; first >= 0 && x <= last; x = (int)(x + space)) axis.push_back(x);
+    const int nax = (int)axis.size();
+    const int64_t L = (int64_t)nax * nax * nax;
+    // the data in FP64 (the threshold test is exact whatever the storage type)
+    double* d = stage();
+    if (ptr_mode_ == GLIA_PTR_HOST_F64) {
+      GLIA_CUDA(cudaMemcpyAsync(d, data, N_ * 8, cudaMemcpyHostToDevice, stream_));
+    } else if (ptr_mode_ == GLIA_PTR_DEVICE_F64) {
+      GLIA_CUDA(cudaMemcpyAsync(d, data, N_ * 8, cudaMemcpyDeviceToDevice, stream_));
+    } else {
+      k_convert<float, double><<<pw_blocks_, kThreads, 0, stream_>>>(N_, (const float*)data, d);
+      GLIA_LAUNCH_CHECK();
+    }
+    int* dax = dalloc<int>(std::max(nax, 1));
+    int* doffs = dalloc<int>(std::max<int64_t>((int64_t)offs.size(), 1));
+    int* dcnt = dalloc<int>(std::max<int64_t>(L, 1));
+    std::vector<int> cnt((size_t)L);
+    if (L > 0) {
+      GLIA_CUDA(cudaMemcpyAsync(dax, axis.data(), nax * sizeof(int), cudaMemcpyHostToDevice,
+                                stream_));
+      GLIA_CUDA(cudaMemcpyAsync(doffs, offs.data(), offs.size() * sizeof(int),
+                                cudaMemcpyHostToDevice, stream_));
+      const int blocks = (int)std::min<int64_t>((L + kThreads - 1) / kThreads, pw_blocks_);
+      k_data_centers<<<blocks, kThreads, 0, stream_>>>(d, n, dax, nax, doffs, interior, thr, dcnt);
+      GLIA_LAUNCH_CHECK();
+      GLIA_CUDA(cudaMemcpyAsync(cnt.data(), dcnt, L * sizeof(int), cudaMemcpyDeviceToHost,
+                                stream_));
+    }
+    if (frac) {
+      fill(tmp_, 0.0);
+      if (L > 0) {
+        const int blocks = (int)std::min<int64_t>((L + kThreads - 1) / kThreads, pw_blocks_);
+        k_data_frac<R><<<blocks, kThreads, 0, stream_>>>(dcnt, n, dax, nax, (double)interior,
+                                                          tmp_);
+        GLIA_LAUNCH_CHECK();
+      }
+      export_field(tmp_, frac);
+    }
+    GLIA_CUDA(cudaStreamSynchronize(stream_));
+    for (void* p : {(void*)dax, (void*)doffs, (void*)dcnt}) dfree(p);
+    int count = 0;
+    for (int64_t t = 0; t < L; t++) {
+      if (!(cnt[(size_t)t] > gvf * interior)) continue;
+      if (count < max_centers) {
+        centers[3 * count] = axis[(size_t)(t / ((int64_t)nax * nax))] * h;
+        centers[3 * count + 1] = axis[(size_t)((t / nax) % nax)] * h;
+        centers[3 * count + 2] = axis[(size_t)(t % nax)] * h;
+      }
+      count++;
+    }
+    *np_out = count;
+    if (count > max_centers)
+      throw Error(GLIA_ERR_INVALID, "phi_data_centers: " + std::to_string(count) +
+                                        " centres found, room for " + std::to_string(max_centers));
+  }
+
   // ------------------------------------------------------------------------------------------
   // observation operator, initial condition
   // ------------------------------------------------------------------------------------------

@@ -852,6 +852,38 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// checkTumorExistence (src/mat/Phi.cpp:457-520) for every lattice point of Phi::setGaussians(Vec
+// data): counts[t] = number of ball offsets o (|o| <= r, from offs) with the point + o inside the
+// grid and data > thr there. Lattice point t = (a, b, c) in x-major order over axis[0 .. nax).
+static __global__ void __launch_bounds__(kThreads)
+    k_data_centers(const double* __restrict__ data, int n, const int* __restrict__ axis, int nax,
+                   const int* __restrict__ offs, int noff, double thr, int* __restrict__ counts) {
+  const int64_t L = (int64_t)nax * nax * nax;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < L;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int x = axis[t / ((int64_t)nax * nax)], y = axis[(t / nax) % nax], z = axis[t % nax];
+    int c = 0;
+    for (int o = 0; o < noff; o++) {
+      const int i = x + offs[3 * o], j = y + offs[3 * o + 1], k = z + offs[3 * o + 2];
+      if (i < 0 || j < 0 || k < 0 || i >= n || j >= n || k >= n) continue;
+      if (data[((int64_t)i * n + j) * n + k] > thr) c++;
+    }
+    counts[t] = c;
+  }
+}
+
+// num_tumor_output of Phi::setGaussians(Vec data): counts / interior at the lattice points
+template <typename R>
+__global__ void k_data_frac(const int* __restrict__ counts, int n, const int* __restrict__ axis,
+                            int nax, double interior, R* __restrict__ out) {
+  const int64_t L = (int64_t)nax * nax * nax;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < L;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int x = axis[t / ((int64_t)nax * nax)], y = axis[(t / nax) % nax], z = axis[t % nax];
+    out[((int64_t)x * n + y) * n + z] = (R)((double)counts[t] / interior);
+  }
+}
+
 // Phi::apply: out = scale * sum_i p_i phi_i, gathered per output cell (cells of 8^3 voxels, box
 // lists in CSR order of increasing index), each output voxel written exactly once.
 template <typename R>

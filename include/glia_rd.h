@@ -163,6 +163,20 @@ int glia_set_phi(glia_ctx* ctx, const double* centers, int np, double sigma,
 int glia_phi_apply(glia_ctx* ctx, const double* p, void* c0);
 /* Phi::applyTranspose (src/mat/Phi.cpp:379-439): pout = Phi^T v. */
 int glia_phi_apply_transpose(glia_ctx* ctx, const void* v, double* pout);
+/* Phi::setGaussians(Vec data) (src/mat/Phi.cpp:615-1004, checkTumorExistence :457-520) for one
+ * process: Gaussian centres placed where the data has tumour. Lattice points X (each axis from
+ * the first to the last index with fmod(X, space) == 0, advancing by X += space on an integer;
+ * space = spacing_factor * sigma / h voxels) keep a centre when more than
+ * gaussian_vol_frac * (grid points of the ball of radius sigma / h) points of the ball around
+ * them, clipped to the grid, hold data > data_threshold (compared in FP64). data is in the
+ * context's pointer mode. centers receives up to max_centers (x, y, z) triples in [0, 2 pi),
+ * in the reference's x-major order; *np_out the number found (GLIA_ERR_INVALID, with *np_out
+ * set, when it exceeds max_centers). frac (may be NULL; pointer mode) receives the
+ * reference's num_tumor_output: count / ball size at the lattice points, 0 elsewhere.
+ * sigma > 0, gaussian_vol_frac >= 0 and a spacing of at least one voxel are required. */
+int glia_phi_data_centers(glia_ctx* ctx, const void* data, double sigma, double data_threshold,
+                          double gaussian_vol_frac, double spacing_factor, int max_centers,
+                          double* centers, int* np_out, void* frac);
 
 /* ---- observation operator ------------------------------------------------------------------ */
 /* Obs::setDefaultFilter (src/mat/Obs.cpp:26-55): filter = [data > thr]. */

@@ -1396,6 +1396,64 @@ int oracle_glia_phi_mesh(int np, const double cm[3], double sigma, double spacin
   }
   return GLIA_OK;
 }
+// Phi::setGaussians(Vec data) (src/mat/Phi.cpp:615-1004) on one process, where every lattice point
+// is local and the neighbour exchange sends nothing: gaussian_interior from the offset loops
+// (:646-653), the first and last lattice index (:679-712), the lattice loops with x += space on
+// an int (:717-719), checkTumorExistenceOutOfProc's clipped ball count (:486-520; with one
+// process every point is in range exactly when it lies on the grid), the selection
+// marker > gvf * interior in index order with X * h coordinates (:870-891) and
+// num_tumor_output = marker / interior (:871).
+int oracle_glia_phi_data_centers(glia_ctx* ctx, const double* data, double sigma, double thr,
+                                 double gvf, double spacing_factor, int max_centers,
+                                 double* centers, int* np_out, double* frac) {
+  if (!ctx || !data || !np_out || max_centers < 0 || (max_centers > 0 && !centers))
+    return GLIA_ERR_INVALID;
+  const int n = ctx->n;
+  const double hx = 2.0 * M_PI / n;
+  const double space = spacing_factor * sigma / hx;
+  if (!(sigma > 0) || !(space >= 1.0) || !(gvf >= 0)) return GLIA_ERR_INVALID;
+  int gaussian_interior = 0;
+  for (int i = -sigma / hx; i <= sigma / hx; i++)
+    for (int j = -sigma / hx; j <= sigma / hx; j++)
+      for (int k = -sigma / hx; k <= sigma / hx; k++)
+        if (std::sqrt((double)(i * i + j * j + k * k)) <= sigma / hx) gaussian_interior++;
+  std::vector<int> marker((size_t)ctx->N, 0);
+  int start = -1, end = -1;
+  for (int x = 0; x < n && start < 0; x++)
+    if (std::fmod((double)x, space) == 0) start = x;
+  for (int x = n - 1; x >= 0 && end < 0; x--)
+    if (std::fmod((double)x, space) == 0) end = x;
+  const double radius = sigma / hx;
+  for (int x = start; start >= 0 && x <= end; x += space)
+    for (int y = start; y <= end; y += space)
+      for (int z = start; z <= end; z += space) {
+        int num_tumor = 0;
+        for (int i = x - radius; i <= x + radius; i++)
+          for (int j = y - radius; j <= y + radius; j++)
+            for (int k = z - radius; k <= z + radius; k++) {
+              if (i < 0 || j < 0 || k < 0 || i >= n || j >= n || k >= n) continue;
+              const double distance =
+                  std::sqrt((double)((i - x) * (i - x) + (j - y) * (j - y) + (k - z) * (k - z)));
+              if (distance <= radius && data[((int64_t)i * n + j) * n + k] > thr) num_tumor++;
+            }
+        marker[((size_t)x * n + y) * n + z] = num_tumor;
+      }
+  int count = 0;
+  for (int64_t i = 0; i < ctx->N; i++) {
+    if (frac) frac[i] = (double)marker[(size_t)i] / gaussian_interior;
+    if (marker[(size_t)i] > gvf * gaussian_interior) {
+      const int64_t X = i / ((int64_t)n * n), Y = (i / n) % n, Z = i % n;
+      if (count < max_centers) {
+        centers[3 * count] = X * hx;
+        centers[3 * count + 1] = Y * hx;
+        centers[3 * count + 2] = Z * hx;
+      }
+      count++;
+    }
+  }
+  *np_out = count;
+  return count > max_centers ? GLIA_ERR_INVALID : GLIA_OK;
+}
 // Raw FFT access for the numpy cross-check.
 int oracle_fft_r2c(int n, const double* in, double* out_interleaved) {
   orc::FFT3 f;

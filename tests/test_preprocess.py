@@ -85,3 +85,32 @@ def test_edema_observation_mask():
     tc = np.array([1.0, 0.0, 0.0, 1.0, 0.5])
     ed = np.array([0.0, 1.0, 0.0, 1.0, 0.0])
     assert np.array_equal(edema_observation_mask(tc, ed, 0.3), [1.0, 0.0, 0.3, 1.0, 0.3])
+
+
+@pytest.mark.parametrize("n,r_vox,frac,sf", [(32, 1.0, 0.0, 2.0), (32, 1.5, 0.2, 2.0),
+                                             (64, 2.0, 0.1, 2.0), (32, 2.0, 0.0, 1.5)])
+def test_oracle_restatement_matches_numpy(n, r_vox, frac, sf):
+    """The FP64 oracle's C++ restatement of the reference's loops (oracle_glia_phi_data_centers)
+    and the numpy version give the same centres and the same tumour-fraction field."""
+    from oracle import oracle
+
+    data = _blobs(n, 7)
+    sigma = r_vox * 2 * math.pi / n
+    o = oracle.context(n)
+    c_o, f_o = o.phi_data_centers(data.reshape(-1), sigma, 0.05, frac, sf, with_frac=True)
+    c_n, _, f_n = data_driven_centers(data, sigma, 0.05, frac, spacing_factor=sf)
+    assert len(c_n) > 0
+    assert np.array_equal(c_o, c_n)
+    assert np.array_equal(f_o.reshape(n, n, n), f_n)
+
+
+def test_oracle_refuses_bad_centre_settings():
+    from glia_gb300.context import GliaError
+    from oracle import oracle
+
+    o = oracle.context(16)
+    data = np.zeros(16 ** 3)
+    with pytest.raises(GliaError):
+        o.phi_data_centers(data, 2 * math.pi / 16, 0.05, -0.1)      # negative volume fraction
+    with pytest.raises(GliaError):
+        o.phi_data_centers(data, 0.1 * 2 * math.pi / 16, 0.05, 0.0)  # spacing below one voxel
