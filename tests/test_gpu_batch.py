@@ -34,9 +34,9 @@ def test_autotune_writes_a_schedule(tmp_path):
 def test_graph_batch_equals_single_problem_runs():
     """One CUDA graph over uneven problems (glia_batch_*): every grouping of the branches gives
     each problem's (J, dJ) bit for bit as its own ordinary evaluation, launch after launch."""
-    probs = gb.default_batch(nt=3, sizes=(32, 64, 32, 128, 64))
+    probs = gb.default_batch(nt=3, sizes=(32, 64, 32, 128, 64, 256))
     b = gb.Batch(probs)
-    b.set_geometry({"32": (2, 1), "64": (2, 1), "128": (8, 4)})
+    b.set_geometry({"32": (2, 1), "64": (2, 1), "128": (8, 4), "256": (8, 4)})
     g = gb.GraphBatch(b)
     try:
         for name, grp in gb.groupings(probs).items():

@@ -173,3 +173,37 @@ def test_gradient_256_central_differences():
     print(json.dumps(out))
     # GB300, FP64, data of this path's own forward: worst direction 3.3e-5 (kappa dominates)
     assert out["max_rel_err"] <= 1e-4
+
+
+@pytest.mark.skipif(os.environ.get("GLIA_SLOW") != "1",
+                    reason="opt-in (GLIA_SLOW=1): one FP64 evaluation at 256^3 with 1000 Gaussians")
+def test_gradient_256_1000_gaussians_mixed_vs_fp64():
+    """The 256^3 reconstruction's problem (1000 Gaussians at the first in-brain lattice points,
+    5 active, rho = 10, kappa = 0.05, nt = 100, checkpoints every 10): the mixed path's gradient
+    at the reconstruction's starting point and at the truth against the FP64 path's, <= 1e-4."""
+    import json
+
+    from glia_gb300.inversion import reconstruction_256
+
+    wl, tissue, centers, x_true, _ = reconstruction_256()
+    gen = gpu(256, FP64)
+    syn.setup_context(gen, wl, tissue, centers, _abi.GLIA_HISTORY_CHECKPOINT, 10)
+    gen.set_coefficients(k=wl.kappa, rho=wl.rho, k_gm_wm=wl.k_gm_wm)
+    d1 = gen.solve_state(gen.phi_apply(x_true[:-2]))
+    x0 = np.concatenate([np.zeros(len(centers)), [0.5 * wl.kappa, 0.5 * wl.rho]])
+    x0[:len(centers)] = 0.1 * (x_true[:-2] > 0)
+    out = {}
+    for name, x in (("start", x0), ("truth_perturbed", x_true * 1.05)):
+        got = {}
+        for prec in (MIXED, FP64):
+            g = gen if prec == FP64 else gpu(256, MIXED)
+            if prec == MIXED:
+                syn.setup_context(g, wl, tissue, centers, _abi.GLIA_HISTORY_CHECKPOINT, 10)
+            g.set_obs_filter(np.ones(256 ** 3))
+            got[prec] = g.eval_objective_and_gradient(x, d1)
+        (Jm, gm), (Jd, gd) = got[MIXED], got[FP64]
+        out[name] = {"J_rel": abs(Jm - Jd) / abs(Jd),
+                     "grad_rel": float(np.linalg.norm(gm - gd) / np.linalg.norm(gd))}
+    print(json.dumps(out))
+    for v in out.values():
+        assert v["grad_rel"] <= 1e-4 and v["J_rel"] <= 1e-4
