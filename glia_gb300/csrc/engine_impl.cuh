@@ -436,14 +436,9 @@ class Engine final : public EngineBase {
   template <int NN, int EPI, bool IN2>
   void xfwd_n(const R* G, const R* aux_in, const R* cx, R* out, R* aux_out, R scale, int blocks) {
     if constexpr (std::is_same<R, float>::value) {
-      if constexpr (IN2) {
-        if (xfwd_ring_)
-          k_xfwd_ring<NN, EPI><<<blocks, 256, xfwd_ring_smem_bytes<NN>(), stream_>>>(
-              g_, G, aux_in, cx, out, aux_out, scale, sc_, ws_, tw256_);
-        else
-          k_xfwd_own<NN, EPI><<<blocks, 256, xfwd_own_smem_bytes<NN>(), stream_>>>(
-              g_, G, aux_in, cx, out, aux_out, scale, sc_, ws_, tw256_);
-      }
+      if constexpr (IN2)
+        k_xfwd_own<NN, EPI><<<blocks, 256, xfwd_own_smem_bytes<NN>(), stream_>>>(
+            g_, G, aux_in, cx, out, aux_out, scale, sc_, ws_, tw256_);
       else
         k_xfwd<NN, EPI><<<blocks, 256, 0, stream_>>>(g_, G, aux_in, cx, out, aux_out, scale, sc_,
                                                      ws_, tw256_);
@@ -510,17 +505,9 @@ class Engine final : public EngineBase {
         xres_inv_ = sms_ * std::min(per_sm(k_xinv<NN, 0, true>, xinv_smem_bytes<NN, 0>()),
                                     per_sm(k_xinv<NN, 1, true>, xinv_smem_bytes<NN, 1>()));
         constexpr int fs = xfwd_own_smem_bytes<NN>();
-        // forward x pass: two staging slots and a separate exchange buffer, or a ring of three
-        // slots with the exchange in the consumed slot (GLIA_XFWD_RING=1)
-        const char* xr = std::getenv("GLIA_XFWD_RING");
-        xfwd_ring_ = xr && xr[0] == '1';
-        constexpr int rs = xfwd_ring_smem_bytes<NN>();
-        xres_fwd_ = sms_ * (xfwd_ring_ ? std::min({per_sm(k_xfwd_ring<NN, EPI_APPLYD>, rs),
-                                                   per_sm(k_xfwd_ring<NN, EPI_SETUP>, rs),
-                                                   per_sm(k_xfwd_ring<NN, EPI_CGW>, rs)})
-                                       : std::min({per_sm(k_xfwd_own<NN, EPI_APPLYD>, fs),
-                                                   per_sm(k_xfwd_own<NN, EPI_SETUP>, fs),
-                                                   per_sm(k_xfwd_own<NN, EPI_CGW>, fs)}));
+        xres_fwd_ = sms_ * std::min({per_sm(k_xfwd_own<NN, EPI_APPLYD>, fs),
+                                     per_sm(k_xfwd_own<NN, EPI_SETUP>, fs),
+                                     per_sm(k_xfwd_own<NN, EPI_CGW>, fs)});
         // y-inverse rows staged by bulk copies (default) or per-thread cp.async
         // (GLIA_YINV_BULK=0)
         const char* yb = std::getenv("GLIA_YINV_BULK");
@@ -2444,7 +2431,6 @@ class Engine final : public EngineBase {
   bool zpass2_ = true;               // z pass with two real lines per complex transform
   bool yinv_bulk_ = true;            // y-inverse rows staged by bulk copies
   bool own_ = false;  // own y and z passes (x pass on): no cuFFT inside the D apply
-  bool xfwd_ring_ = false;  // forward x pass through a ring of three slots (k_xfwd_ring)
   // graph-captured evaluations (eval_prepare / eval_capture / eval_finish)
   bool capture_ = false, cap_ready_ = false;
   cudaStream_t cap_side_ = nullptr;  // captures the PCG loop bodies

@@ -242,50 +242,6 @@ __device__ __forceinline__ void xdft(float2* sm, const float2* twb, int c, int g
   __syncthreads();
 }
 
-// xdft on a tile staged in shared memory, with the exchange in the tile's own slot: every input
-// is read into registers first, a CTA barrier, then the slot serves as the exchange buffer; the
-// final barrier frees the slot. out(m2, k1, k2, y) as in xdft.
-template <class D, int S, class Out>
-__device__ __forceinline__ void xdft_inslot(float2* sl, const float2* twb, int c, int gi,
-                                            Out&& out) {
-  constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
-  constexpr int NB1 = R2 / GR, NB2 = R1 / GR;
-  float2 u[NB1][R1];
-#pragma unroll
-  for (int m = 0; m < NB1; m++) {
-    const int b = gi + GR * m;
-#pragma unroll
-    for (int a = 0; a < R1; a++) u[m][a] = sl[(R2 * a + b) * T + c];
-  }
-  __syncthreads();  // the slot's inputs are in registers: it becomes the exchange buffer
-#pragma unroll
-  for (int m = 0; m < NB1; m++) {
-    const int b = gi + GR * m;
-    reg_dft<R1, S>(u[m]);
-    const float4* w4 = reinterpret_cast<const float4*>(twb + b * R1);
-#pragma unroll
-    for (int k1 = 0; k1 < R1; k1 += 2) {
-      const float4 w = w4[k1 / 2];
-      if (k1) u[m][k1] = cmul2(u[m][k1], make_float2(w.x, w.y));
-      u[m][k1 + 1] = cmul2(u[m][k1 + 1], make_float2(w.z, w.w));
-      sl[(k1 * R2 + b) * T + c] = u[m][k1];
-      sl[((k1 + 1) * R2 + b) * T + c] = u[m][k1 + 1];
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int m2 = 0; m2 < NB2; m2++) {
-    const int k1 = gi + GR * m2;
-    float2 y[R2];
-#pragma unroll
-    for (int b = 0; b < R2; b++) y[b] = sl[(k1 * R2 + b) * T + c];
-    reg_dft<R2, S>(y);
-#pragma unroll
-    for (int k2 = 0; k2 < R2; k2++) out(m2, k1, k2, y[k2]);
-  }
-  __syncthreads();  // the exchange is read: the slot is free
-}
-
 // MODE 0: spectrum src -> G; MODE 1: PCG direction p = P r + b p (r = src, p = pdir, p written).
 // The y and z gradient spectra differ from the plain spectrum only by factors constant along x,
 // so two x transforms give the three components: G_x = F^-1(i w_x u) / N and
@@ -489,110 +445,6 @@ __global__ void __launch_bounds__(256, 2)
     }
   }
   xfwd_finish<EPI>(acc, g, sc, ws, cx != nullptr);
-}
-
-// k_xfwd_own with a ring of three slots: item i (M_x, M_r, then the epilogue's spectra of each
-// tile in turn) sits in slot i % 3 and is staged when item i - 3 has been consumed, so every
-// item is in flight for about one tile; the DFT exchanges run in the item's own slot
-// (xdft_inslot), which keeps the shared memory at three tiles.
-template <int NN, int EPI>
-__global__ void __launch_bounds__(256, 2)
-    k_xfwd_ring(Geo g, const float* __restrict__ M2, const float* __restrict__ aux_in,
-                const float* __restrict__ cx, float* __restrict__ out, float* __restrict__ aux_out,
-                float scale, DevScalars* __restrict__ sc, RedWs ws,
-                const float2* __restrict__ tw_g) {
-  using D = XDecomp<NN>;
-  constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
-  constexpr int NB2 = R1 / GR;
-  extern __shared__ float4 xfwd_dyn[];
-  float2* slots = reinterpret_cast<float2*>(xfwd_dyn);  // 3 x NN * T
-  float2* tw = slots + 3 * NN * T;
-  if (EPI == EPI_CGW && sc->status != 0) return;
-  fill_twb<D, -1>(tw, tw_g);
-  const int c = threadIdx.x % T, gi = threadIdx.x / T;
-  const int plane = NN * g.nh, Ns = plane * NN;
-  const int ntiles = plane / T;
-  const float a = EPI == EPI_APPLYD ? 0.f : (float)sc->a_cn;
-  const float pcc = (float)sc->pc_c;
-  const float invN = (float)g.invN;
-  const float2* Mx = reinterpret_cast<const float2*>(M2);
-  const float2* Mr = Mx + Ns;
-  const float2* AX = reinterpret_cast<const float2*>(aux_in);
-  const float2* CX = reinterpret_cast<const float2*>(cx);
-  float2* O = reinterpret_cast<float2*>(out);
-  float2* AO = reinterpret_cast<float2*>(aux_out);
-  const int naux = EPI == EPI_APPLYD ? 0 : (EPI == EPI_SETUP && CX ? 2 : 1);
-  const int NI = 2 + naux;
-  const int mytiles =
-      (int)blockIdx.x < ntiles ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
-                               : 0;
-  const int nitems = NI * mytiles;
-  auto slot = [&](int i) { return slots + (i % 3) * NN * T; };
-  auto issue = [&](int i) {  // after a CTA barrier that ends every use of the slot
-    if (i < nitems) {
-      const int t = (int)blockIdx.x + (i / NI) * (int)gridDim.x, kind = i % NI;
-      const float2* src = kind == 0 ? Mx : (kind == 1 ? Mr : (kind == 2 ? AX : CX));
-      stage_tile<NN, T>(slot(i), src, plane, t);
-    }
-    cp_async_commit();
-  };
-  issue(0);
-  issue(1);
-  issue(2);
-  Acc<float> acc[4];
-  for (int it = 0; it < mytiles; it++) {
-    const int tile = (int)blockIdx.x + it * (int)gridDim.x;
-    const int i0 = NI * it;
-    const XCol col = xcol(g, tile * T + c);
-    float2 dsum[NB2][R2];
-    cp_async_wait<2>();  // item i0 (groups i0 + 1, i0 + 2 may still be in flight)
-    __syncthreads();
-    xdft_inslot<D, -1>(slot(i0), tw, c, gi, [&](int m2, int k1, int k2, float2 y) {
-      const float w = (float)wavenum(k1 + R1 * k2, NN);
-      dsum[m2][k2] = make_float2(-w * y.y, w * y.x);
-    });
-    issue(i0 + 3);
-    cp_async_wait<2>();  // item i0 + 1
-    __syncthreads();
-    xdft_inslot<D, -1>(slot(i0 + 1), tw, c, gi, [&](int m2, int, int k2, float2 y) {
-      dsum[m2][k2].x += y.x;
-      dsum[m2][k2].y += y.y;
-    });
-    issue(i0 + 4);
-    if (naux) {
-      if (naux == 2)
-        cp_async_wait<1>();  // items i0 + 2 and i0 + 3
-      else
-        cp_async_wait<2>();  // item i0 + 2
-      __syncthreads();
-    }
-    const float2* SA = slot(i0 + 2);
-    const float2* SX = slot(i0 + 3);
-#pragma unroll
-    for (int m2 = 0; m2 < NB2; m2++) {
-      const int k1 = gi + GR * m2;
-#pragma unroll
-      for (int k2 = 0; k2 < R2; k2++) {
-        const int kx = k1 + R1 * k2;
-        const float2 av = naux ? SA[kx * T + c] : make_float2(0.f, 0.f);
-        const float2 xv = naux == 2 ? SX[kx * T + c] : make_float2(0.f, 0.f);
-        xfwd_epilogue<NN, EPI>(dsum[m2][k2], kx, kx * plane + col.q, col, a, pcc, invN, scale, av,
-                               xv, naux == 2, O, AO, acc);
-      }
-    }
-    if (naux) {
-      __syncthreads();  // the epilogue's slots are read
-      issue(i0 + 5);
-      if (naux == 2) issue(i0 + 6);
-    }
-  }
-  cp_async_wait<0>();
-  xfwd_finish<EPI>(acc, g, sc, ws, naux == 2);
-}
-
-template <int NN>
-constexpr int xfwd_ring_smem_bytes() {
-  return (3 * NN * XDecomp<NN>::T + 256) * (int)sizeof(float2);
 }
 
 template <int NN>
