@@ -148,11 +148,17 @@ def _data256(g, wl):
 def test_gradient_256_central_differences():
     """DerivativeOperators::checkGradient's protocol (src/grad/DerivativeOperators.cpp:369-450)
     on the 256^3 workload: central differences (h = 1e-3) of J along 8 random unit directions
-    (seed 3) against the adjoint gradient, FP64 fused path, PCG rtol 1e-10 so that the PCG
-    tolerance stays below the difference quotient's resolution. The p block is the exact
-    discrete adjoint; kappa and rho are the reference's trapezoid quadratures."""
+    (seed 3) against the adjoint gradient taken through the torch.autograd.Function
+    (glia_gb300.autograd.rd_objective, the data a CUDA tensor: the device-pointer path), FP64
+    fused path, PCG rtol 1e-10 so that the PCG tolerance stays below the difference quotient's
+    resolution. The p block is the exact discrete adjoint; kappa and rho are the reference's
+    trapezoid quadratures."""
     import json
     import time
+
+    import torch
+
+    from glia_gb300 import autograd as ga
 
     wl = syn.GradientWorkload(n=256, nt=100)
     tissue = wl.tissue()
@@ -162,16 +168,23 @@ def test_gradient_256_central_differences():
     g.set_obs_filter(np.ones(256 ** 3))
     g.set_pcg(1e-10, 5000)
     d1, source = _data256(g, wl)
+    steady_pc(g, wl.dt)
+    d1_dev = torch.tensor(d1, dtype=torch.float64, device="cuda")
     x = wl.x_eval()
     t0 = time.time()
-    J, grad = g.eval_objective_and_gradient(x, d1)
+    xt = torch.tensor(x, requires_grad=True)
+    Jt = ga.rd_objective(xt, g, d1_dev)
+    Jt.backward()
+    J, grad = float(Jt), xt.grad.numpy().copy()
     rng = np.random.default_rng(3)
     h, np_ = 1e-3, wl.n_gauss
     rows = []
     for _ in range(8):
         d = rng.standard_normal(x.size)
         d /= np.linalg.norm(d)
-        fd = (g.eval_objective(x + h * d, d1) - g.eval_objective(x - h * d, d1)) / (2 * h)
+        Jp = float(ga.rd_objective(torch.tensor(x + h * d), g, d1_dev))
+        Jm = float(ga.rd_objective(torch.tensor(x - h * d), g, d1_dev))
+        fd = (Jp - Jm) / (2 * h)
         ad = float(grad @ d)
         rows.append({"fd": fd, "adjoint": ad, "rel_err": abs(fd - ad) / abs(fd),
                      "p_part": float(grad[:np_] @ d[:np_]),
