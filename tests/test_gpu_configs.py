@@ -175,7 +175,7 @@ def test_gradient_256_central_differences():
     xt = torch.tensor(x, requires_grad=True)
     Jt = ga.rd_objective(xt, g, d1_dev)
     Jt.backward()
-    J, grad = float(Jt), xt.grad.numpy().copy()
+    J, grad = float(Jt.detach()), xt.grad.numpy().copy()
     rng = np.random.default_rng(3)
     h, np_ = 1e-3, wl.n_gauss
     rows = []
