@@ -469,17 +469,10 @@ class Engine final : public EngineBase {
       else if (which == 0)
         k_yinv<NN><<<std::min(own_res_[0], pw_blocks_), 256, yinv_smem_bytes<NN>(), stream_>>>(
             g3r_, g3s_, tw256_);
-      else if (which == 1 && zpass2_) {
-        if constexpr (NN == 256) {
-          if (zshfl_) {
-            k_zpass2<NN, true><<<std::min(own_res_[1], pw_blocks_), 256,
-                                 zpass2_smem_bytes<NN>(), stream_>>>(g3s_, kxx_, tw256_);
-            return;
-          }
-        }
+      else if (which == 1 && zpass2_)
         k_zpass2<NN><<<std::min(own_res_[1], pw_blocks_), 256, zpass2_smem_bytes<NN>(),
                        stream_>>>(g3s_, kxx_, tw256_);
-      } else if (which == 1)
+      else if (which == 1)
         k_zpass<NN><<<std::min(own_res_[1], pw_blocks_), 256, zpass_smem_bytes<NN>(), stream_>>>(
             g3s_, kxx_, tw256_);
       else if (tma_)
@@ -525,11 +518,6 @@ class Engine final : public EngineBase {
         // the even/odd half-length version (k_zpass)
         const char* z2 = std::getenv("GLIA_ZPASS2");
         zpass2_ = !(z2 && z2[0] == '0');
-        // 256^3 z pass: the split of the pair transforms by warp shuffles (GLIA_ZSHFL=1)
-        const char* zs = std::getenv("GLIA_ZSHFL");
-        zshfl_ = NN == 256 && zs && zs[0] == '1';
-        if constexpr (NN == 256)
-          if (zshfl_) per_sm(k_zpass2<NN, true>, zpass2_smem_bytes<NN>());
         own_res_[1] = sms_ * (zpass2_ ? per_sm(k_zpass2<NN>, zpass2_smem_bytes<NN>())
                                       : per_sm(k_zpass<NN>, zpass_smem_bytes<NN>()));
         const char* te = std::getenv("GLIA_TMA");
@@ -2443,7 +2431,6 @@ class Engine final : public EngineBase {
   bool zpass2_ = true;               // z pass with two real lines per complex transform
   bool yinv_bulk_ = true;            // y-inverse rows staged by bulk copies
   bool own_ = false;  // own y and z passes (x pass on): no cuFFT inside the D apply
-  bool zshfl_ = false;  // 256^3 z pass with the pair split by warp shuffles
   // graph-captured evaluations (eval_prepare / eval_capture / eval_finish)
   bool capture_ = false, cap_ready_ = false;
   cudaStream_t cap_side_ = nullptr;  // captures the PCG loop bodies

@@ -77,12 +77,9 @@ __device__ __forceinline__ void stage_lines2(float2* slot, const char* src) {
 }
 
 // One complex pair line through F^-1, the k multiply and F. u holds Z[R2 a + t] on entry; mulk
-// (ii, k2, z) returns z times k at position t + R2 ii + R1 k2; out(ii, k2, A', B', zh) receives
-// the split result at q = t + R2 ii + R1 k2 for q < n/2 and, on thread t = 0, zh = Z'[n/2].
-// E0 / E1: the group's exchange halves. SHFL (n = 256, one group = half a warp, one stage-2 row
-// per thread): the split takes Z'[n - q] from the partner lane 16 - t (register 15 - k2; thread
-// 0 from its own registers) by warp shuffles instead of a round trip through shared memory.
-template <int NN, bool SHFL, class MulK, class Out>
+// (ii, k2, z) returns z times k at position t + R2 ii + R1 k2; out(ii, k2, A', B') receives the
+// split result at q = t + R2 ii + R1 k2 for q < n/2. E0 / E1: the group's exchange halves.
+template <int NN, class MulK, class Out>
 __device__ __forceinline__ void pair_line(float2* E0, float2* E1, const float4* twr, int t,
                                           float2 (&u)[Z2Geom<NN>::R1], MulK&& mulk, Out&& out) {
   using Z = Z2Geom<NN>;
@@ -135,24 +132,6 @@ __device__ __forceinline__ void pair_line(float2* E0, float2* E1, const float4* 
     for (int tp = 0; tp < R2; tp++) v[ii][tp] = r[tp ^ (k1 & (R2 - 1))];
     reg_dft<R2, -1>(v[ii]);  // v[ii][k2] = Z'[k1 + R1 k2]
   }
-  if constexpr (SHFL) {
-    static_assert(NN == 256 && R2 == 16 && KPT == 1, "the shuffle split is laid out for n = 256");
-    const int lane = threadIdx.x & 31;
-    const int partner = (lane & 16) | ((16 - t) & 15);
-    const float2 zh = v[0][8];  // Z'[n/2] on thread 0
-#pragma unroll
-    for (int k2 = 0; k2 < 8; k2++) {
-      const float2 send = v[0][15 - k2];
-      float2 zq = make_float2(__shfl_sync(0xffffffffu, send.x, partner),
-                              __shfl_sync(0xffffffffu, send.y, partner));
-      if (t == 0) zq = v[0][(16 - k2) & 15];
-      const float2 z = v[0][k2];
-      const float2 A = make_float2(0.5f * (z.x + zq.x), 0.5f * (z.y - zq.y));
-      const float2 B = make_float2(0.5f * (z.y + zq.y), -0.5f * (z.x - zq.x));
-      out(0, k2, A, B, zh);
-    }
-    return;
-  }
   __syncwarp();
   // natural order for the split: Z'[q] at e2(q)
   auto e2 = [&](int q) { return q < H ? E0 + q : E1 + (q - H); };
@@ -170,8 +149,7 @@ __device__ __forceinline__ void pair_line(float2* E0, float2* E1, const float4* 
       const float2 z = v[ii][k2], zq = *e2((NN - q) & (NN - 1));
       const float2 A = make_float2(0.5f * (z.x + zq.x), 0.5f * (z.y - zq.y));
       const float2 B = make_float2(0.5f * (z.y + zq.y), -0.5f * (z.x - zq.x));
-      // Z'[n/2] (the start of the second exchange half) only where thread 0 needs it
-      out(ii, k2, A, B, (ii == 0 && k2 == 0 && t == 0) ? *E1 : A);
+      out(ii, k2, A, B);
     }
 }
 
@@ -179,7 +157,7 @@ __device__ __forceinline__ void pair_line(float2* E0, float2* E1, const float4* 
 // block of LB lines: k, H_x, H_y, H_0, through a ring of three shared-memory slots (item i in
 // slot i % 3). k goes to registers first and its slot takes H_0; the H_x / H_y pairs need both
 // slots; then the next block's k and H_x are staged and H_0 is done; then the next H_y is staged.
-template <int NN, bool SHFL = false>
+template <int NN>
 __global__ void __launch_bounds__(256, 2)
     k_zpass2(float* __restrict__ Hio, const float* __restrict__ kf,
              const float2* __restrict__ tw_g) {
@@ -261,16 +239,18 @@ __global__ void __launch_bounds__(256, 2)
       }
       float2* OX = Hc + (size_t)(blk * LB + l) * NQ;
       float2* OY = OX + NP;
-      pair_line<NN, SHFL>(
+      pair_line<NN>(
           X + sh, Y + sh, twr, t, u,
           [&](int ii, int k2, float2 z) {
             const float kk = kv[j][ii][k2];
             return make_float2(z.x * kk, z.y * kk);
           },
-          [&](int ii, int k2, float2 A, float2 B, float2 zn) {
+          [&](int ii, int k2, float2 A, float2 B) {
             const int q = t + R2 * ii + R1 * k2;
             if (ii == 0 && k2 == 0 && t == 0) {
-              // packed slot 0: (A'[0], A'[n/2]), (B'[0], B'[n/2]), all real (zn = Z'[n/2])
+              // packed slot 0: (A'[0], A'[n/2]), (B'[0], B'[n/2]), all real; Z'[n/2] sits at
+              // the start of the second exchange half
+              const float2 zn = Y[sh];
               A.y = zn.x;
               B.y = zn.y;
             }
@@ -307,12 +287,12 @@ __global__ void __launch_bounds__(256, 2)
       }
       float2* O0 = Hc + (size_t)2 * NP + (size_t)(blk * LB + l0) * NQ;
       float2* O1 = O0 + NQ;
-      pair_line<NN, SHFL>(
+      pair_line<NN>(
           P0 + sh, P1 + sh, twr, t, u,
           [&](int ii, int k2, float2 z) {
             return make_float2(z.x * kv[0][ii][k2], z.y * kv[1][ii][k2]);
           },
-          [&](int ii, int k2, float2 A, float2 B, float2) {
+          [&](int ii, int k2, float2 A, float2 B) {
             const int q = t + R2 * ii + R1 * k2;
             const float w = (float)q;  // L_z = i w A' (0 at q = 0)
             O0[q] = make_float2(-w * A.y, w * A.x);
