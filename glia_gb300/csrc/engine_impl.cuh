@@ -2022,6 +2022,10 @@ class Engine final : public EngineBase {
     capture_ = false;
     cap_total_solves_ = st_.total_diffusion_solves - saved.total_diffusion_solves;
     st_ = saved;
+    // nothing has run yet: the history is valid only once a launch of the graph has been read
+    cap_state_done_ = state_done_;
+    cap_adjoint_done_ = adjoint_done_;
+    state_done_ = adjoint_done_ = false;
   }
   void eval_finish(double* J, double* dJ) override {
     if (!cap_ready_) throw Error(GLIA_ERR_STATE, "eval_finish needs a captured evaluation");
@@ -2046,6 +2050,8 @@ class Engine final : public EngineBase {
     ksp_itr_ = h.it;
     if (h.dev_fault) raise_device_fault();
     if (h.err_status < 0) finish_solve(SolveStatus{h.err_status, h.err_its, h.last_dp});
+    state_done_ = cap_state_done_;  // the launch swept the history as the capture recorded
+    adjoint_done_ = cap_adjoint_done_;
     const double hh = 2.0 * M_PI / g_.n, h3 = hh * hh * hh;
     if (J) *J = h3 * 0.5 * h.m1_keep + cap_reg_;
     if (!dJ) return;
@@ -2433,6 +2439,7 @@ class Engine final : public EngineBase {
   bool own_ = false;  // own y and z passes (x pass on): no cuFFT inside the D apply
   // graph-captured evaluations (eval_prepare / eval_capture / eval_finish)
   bool capture_ = false, cap_ready_ = false;
+  bool cap_state_done_ = false, cap_adjoint_done_ = false;
   cudaStream_t cap_side_ = nullptr;  // captures the PCG loop bodies
   int64_t cap_solves_ = 0, cap_total_solves_ = 0;
   double cap_reg_ = 0;

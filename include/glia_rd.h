@@ -265,8 +265,12 @@ int glia_get_timing(glia_ctx* ctx, int slot, const char** name, int64_t* launche
  * sweeps with its PCG loops as conditional WHILE nodes, a join. group[i] (NULL: all 0) orders
  * the branches: contexts of one group run as parallel branches, groups one after another in
  * increasing order. glia_batch_launch launches the graph once (stream NULL = the batch's own
- * stream); every launch recomputes the evaluations captured at those x and d1 (data can be
- * changed in place between launches; a new x needs a new capture). glia_batch_results waits for
+ * stream); every launch recomputes the evaluations captured at those x and d1 from the
+ * coefficients, Phi p and data that the capture left in each context: a call on a context
+ * between capture and launch that changes them (coefficients, Phi, data, an ordinary
+ * evaluation at another x) changes what the next launch computes, so capture again after such
+ * calls; a new x needs a new capture. Until glia_batch_results has read a launch, the contexts
+ * report no state history (get_state / solve_adjoint refuse). glia_batch_results waits for
  * the launch and writes J[i] and dJ[i] (np + nk + nr entries each; dJ NULL: objectives only).
  * Requirements: the fused engine, one snapshot, phi_store = 0, a history mode other than OFF,
  * timing disabled, every context on its own non-default stream, and one ordinary evaluation of

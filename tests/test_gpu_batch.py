@@ -85,3 +85,22 @@ def test_graph_autotune_writes_a_schedule(tmp_path):
     assert len(choice["group"]) == len(probs)
     table = json.load(open(cache))
     assert "graph:" + gb.signature(probs) in table
+
+
+def test_captured_contexts_report_no_history_until_a_launch_is_read():
+    """After glia_batch_capture nothing has run: the contexts refuse the adjoint (no valid state
+    history) until glia_batch_results has read a launch of the graph."""
+    from glia_gb300.context import GliaError
+
+    probs = gb.default_batch(nt=2, sizes=(32, 32))
+    b = gb.Batch(probs)
+    g = gb.GraphBatch(b)
+    try:
+        pt = np.zeros(32 ** 3)
+        with pytest.raises(GliaError, match="GLIA_ERR_STATE"):
+            b.ctxs[0].solve_adjoint(pt)
+        g.evaluate()
+        b.ctxs[0].solve_adjoint(pt)  # the launch's history is valid now
+    finally:
+        g.close()
+        b.close()
