@@ -429,9 +429,17 @@ def run_reconstruction(n=128, nt=40, precisions=("mixed", "fp64"), every=10, max
            "k_scale": k_scale, "rho_scale": rho_scale}
     data = None
     for name in precisions:
+        if name not in ("mixed", "fp64", "fp64_plain"):
+            raise ValueError(f"unknown arm {name} (mixed, fp64, fp64_plain)")
         prec = _abi.GLIA_MIXED if name == "mixed" else _abi.GLIA_FP64
-        ctx = Context(api, wl.n, prec)
-        syn.setup_context(ctx, wl, tissue, centers, _abi.GLIA_HISTORY_CHECKPOINT, every)
+        # fp64_plain: the reference-structured FP64 engine with the full time history (the plain
+        # FP64 GPU path); the other arms are the fused engine with checkpoints
+        plain = name == "fp64_plain"
+        ctx = Context(api, wl.n, prec, _abi.GLIA_ENGINE_REFERENCE if plain else
+                      _abi.GLIA_ENGINE_FUSED)
+        syn.setup_context(ctx, wl, tissue, centers,
+                          _abi.GLIA_HISTORY_FULL if plain else _abi.GLIA_HISTORY_CHECKPOINT,
+                          0 if plain else every)
         ctx.set_opt(k_scale=k_scale, rho_scale=rho_scale)
         ctx.set_obs_filter(np.ones(wl.n ** 3))
         if data is None:  # data from the FP64 forward at the true parameters
