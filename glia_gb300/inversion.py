@@ -32,6 +32,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import sys
 import time
 from dataclasses import dataclass, field
 
@@ -408,7 +409,7 @@ def reconstruction_256(n=256, nt=100, n_gauss=1000, seed_truth=6):
 
 
 def run_reconstruction(n=128, nt=40, precisions=("mixed", "fp64"), every=10, maxit=100,
-                       problem=None, gatol=0.0):
+                       problem=None, gatol=0.0, progress=False):
     """L-BFGS from p = 0, kappa and rho at half their true values, to a 1e-3 relative reduction
     of the projected gradient (gatol = 0: the relative test alone, as the workload states; the
     reference's default adds gatol = 1e-4). kappa and rho enter x through the reference's
@@ -475,6 +476,8 @@ def run_reconstruction(n=128, nt=40, precisions=("mixed", "fp64"), every=10, max
                      "kappa": float(x[npp]), "kappa_rel_err": abs(x[npp] / x_true[npp] - 1),
                      "rho": float(x[npp + 1]), "rho_rel_err": abs(x[npp + 1] / x_true[npp + 1] - 1)}
         ctx.close()
+        if progress:  # each arm as soon as it ends (a long run cut short keeps the arms done)
+            print(json.dumps({name: out[name]}), file=sys.stderr, flush=True)
     return out
 
 
@@ -490,4 +493,5 @@ if __name__ == "__main__":
     a = ap.parse_args()
     prob = reconstruction_256() if a.full256 else None
     print(json.dumps(run_reconstruction(a.n, a.nt, tuple(a.precisions.split(",")),
-                                        maxit=a.maxit, problem=prob, gatol=a.gatol)))
+                                        maxit=a.maxit, problem=prob, gatol=a.gatol,
+                                        progress=True)))
