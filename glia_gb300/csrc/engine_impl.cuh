@@ -436,14 +436,10 @@ class Engine final : public EngineBase {
   template <int NN, int EPI, bool IN2>
   void xfwd_n(const R* G, const R* aux_in, const R* cx, R* out, R* aux_out, R scale, int blocks) {
     if constexpr (std::is_same<R, float>::value) {
-      if constexpr (IN2) {
-        if (xfwd_ip_)
-          k_xfwd_ip<NN, EPI><<<blocks, 256, xfwd_ip_smem_bytes<NN>(), stream_>>>(
-              g_, G, aux_in, cx, out, aux_out, scale, sc_, ws_, tw256_);
-        else
-          k_xfwd_own<NN, EPI><<<blocks, 256, xfwd_own_smem_bytes<NN>(), stream_>>>(
-              g_, G, aux_in, cx, out, aux_out, scale, sc_, ws_, tw256_);
-      } else
+      if constexpr (IN2)
+        k_xfwd_own<NN, EPI><<<blocks, 256, xfwd_own_smem_bytes<NN>(), stream_>>>(
+            g_, G, aux_in, cx, out, aux_out, scale, sc_, ws_, tw256_);
+      else
         k_xfwd<NN, EPI><<<blocks, 256, 0, stream_>>>(g_, G, aux_in, cx, out, aux_out, scale, sc_,
                                                      ws_, tw256_);
     }
@@ -482,9 +478,6 @@ class Engine final : public EngineBase {
       else if (tma_)
         k_yfwd_tma<NN><<<std::min(own_res_[2], pw_blocks_), 256, yfwd_tma_smem_bytes<NN>(),
                          stream_>>>(kmap_, g3r_, tw256_, sc_);
-      else if (yfwd_ip_)
-        k_yfwd_ip<NN><<<std::min(own_res_[2], pw_blocks_), 256, yfwd_ip_smem_bytes<NN>(),
-                        stream_>>>(g3s_, g3r_, tw256_);
       else
         k_yfwd<NN><<<std::min(own_res_[2], pw_blocks_), 256, yfwd_smem_bytes<NN>(), stream_>>>(
             g3s_, g3r_, tw256_);
@@ -511,21 +504,10 @@ class Engine final : public EngineBase {
       if (own_) {
         xres_inv_ = sms_ * std::min(per_sm(k_xinv<NN, 0, true>, xinv_smem_bytes<NN, 0>()),
                                     per_sm(k_xinv<NN, 1, true>, xinv_smem_bytes<NN, 1>()));
-        // forward x pass exchanging in its input slots, three CTAs per SM (GLIA_XFWD_IP=1),
-        // or through a separate exchange buffer, two CTAs per SM
-        const char* xi = std::getenv("GLIA_XFWD_IP");
-        xfwd_ip_ = xi && xi[0] == '1';
-        if (xfwd_ip_) {
-          constexpr int fs = xfwd_ip_smem_bytes<NN>();
-          xres_fwd_ = sms_ * std::min({per_sm(k_xfwd_ip<NN, EPI_APPLYD>, fs),
-                                       per_sm(k_xfwd_ip<NN, EPI_SETUP>, fs),
-                                       per_sm(k_xfwd_ip<NN, EPI_CGW>, fs)});
-        } else {
-          constexpr int fs = xfwd_own_smem_bytes<NN>();
-          xres_fwd_ = sms_ * std::min({per_sm(k_xfwd_own<NN, EPI_APPLYD>, fs),
-                                       per_sm(k_xfwd_own<NN, EPI_SETUP>, fs),
-                                       per_sm(k_xfwd_own<NN, EPI_CGW>, fs)});
-        }
+        constexpr int fs = xfwd_own_smem_bytes<NN>();
+        xres_fwd_ = sms_ * std::min({per_sm(k_xfwd_own<NN, EPI_APPLYD>, fs),
+                                     per_sm(k_xfwd_own<NN, EPI_SETUP>, fs),
+                                     per_sm(k_xfwd_own<NN, EPI_CGW>, fs)});
         // y-inverse rows staged by bulk copies (default) or per-thread cp.async
         // (GLIA_YINV_BULK=0)
         const char* yb = std::getenv("GLIA_YINV_BULK");
@@ -540,12 +522,8 @@ class Engine final : public EngineBase {
                                       : per_sm(k_zpass<NN>, zpass_smem_bytes<NN>()));
         const char* te = std::getenv("GLIA_TMA");
         tma_ = te && te[0] == '1';
-        // y-forward pass exchanging in its input slots, three CTAs per SM (GLIA_YFWD_IP=1)
-        const char* yi = std::getenv("GLIA_YFWD_IP");
-        yfwd_ip_ = !tma_ && yi && yi[0] == '1';
         own_res_[2] = sms_ * (tma_ ? per_sm(k_yfwd_tma<NN>, yfwd_tma_smem_bytes<NN>())
-                              : yfwd_ip_ ? per_sm(k_yfwd_ip<NN>, yfwd_ip_smem_bytes<NN>())
-                                         : per_sm(k_yfwd<NN>, yfwd_smem_bytes<NN>()));
+                                   : per_sm(k_yfwd<NN>, yfwd_smem_bytes<NN>()));
         // TMA view of the packed arrays K = [K_x, K_y, L_z]: 3 n^2 rows of n floats, tiles of
         // 2T floats x n rows (used by k_yfwd<TMA = true>, GLIA_TMA=1)
         if (tma_)
@@ -2452,8 +2430,6 @@ class Engine final : public EngineBase {
   bool xpass_ = false;   // x pass fused into the spectral kernels (FP32, n = 64 ... 256)
   cufftHandle r2c2d3_ = 0, c2r2d3_ = 0;  // batched 2-D (y, z) transforms, 3n planes
   float2* tw256_ = nullptr;
-  bool xfwd_ip_ = false;  // k_xfwd_ip instead of k_xfwd_own
-  bool yfwd_ip_ = false;  // k_yfwd_ip instead of k_yfwd
   int xres_inv_ = 0, xres_fwd_ = 0;  // resident CTAs of k_xinv / k_xfwd on this device
   int own_res_[3] = {0, 0, 0};       // ... of the y-inverse pass, the z pass, k_yfwd
   CUtensorMap kmap_{};               // TMA map of the packed line arrays (k_yfwd)

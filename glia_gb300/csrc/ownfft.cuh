@@ -410,109 +410,6 @@ __global__ void __launch_bounds__(256, 2)
 }
 
 template <int NN>
-constexpr int yfwd_ip_smem_bytes() {
-  return (2 * NN * YDecomp<NN>::T + 2 * NN + 256) * (int)sizeof(float2);
-}
-
-// k_yfwd with each transform exchanging in its own input slot (xdft_ip): no exchange buffer, so
-// three CTAs fit on an SM at 256^3 (70 KB of shared memory, at most 80 registers per thread).
-// Item i + 2 enters slot i % 2 when the transform of item i has ended.
-template <int NN>
-__global__ void __launch_bounds__(256, 3)
-    k_yfwd_ip(const float* __restrict__ Kin, float* __restrict__ Mout,
-              const float2* __restrict__ tw_g) {
-  using D = YDecomp<NN>;
-  constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T, NB2 = R1 / GR;
-  constexpr int NQ = NN / 2, NH = NN / 2 + 1, CB = NQ / T;
-  constexpr int PS = NN * NH, NS = NN * PS, NP = NN * NN * NQ;
-  constexpr int ntiles = NN * CB;
-  extern __shared__ float4 yfwd_dyn[];
-  float2* slots = reinterpret_cast<float2*>(yfwd_dyn);  // 2 x NN * T
-  float2* zA = slots + 2 * NN * T;
-  float2* zB = zA + NN;
-  float2* tw = zB + NN;
-  fill_twb<D, -1>(tw, tw_g);
-  const int c = threadIdx.x % T, gi = threadIdx.x / T;
-  const float2* K = reinterpret_cast<const float2*>(Kin);
-  float2* Mx = reinterpret_cast<float2*>(Mout);
-  float2* Mr = Mx + NS;
-  const int mytiles =
-      (int)blockIdx.x < ntiles ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
-                               : 0;
-  const int nitems = 3 * mytiles;
-  auto issue = [&](int i) {
-    if (i < nitems) {
-      const int t = (int)blockIdx.x + (i / 3) * (int)gridDim.x, j = i % 3;
-      const int x = t / CB, cb = t - x * CB;
-      stage_tile<NN, T>(slots + (i & 1) * NN * T, K + (size_t)j * NP + (size_t)x * NN * NQ, NQ, cb);
-    }
-    cp_async_commit();
-  };
-  issue(0);
-  issue(1);
-  for (int it = 0; it < mytiles; it++) {
-    const int tile = (int)blockIdx.x + it * (int)gridDim.x;
-    const int x = tile / CB, cb = tile - x * CB, kz = cb * T + c;
-    const bool pk = kz == 0;
-    const int i0 = 3 * it;
-    auto slot = [&](int i) { return slots + (i & 1) * NN * T; };
-    cp_async_wait<1>();
-    __syncthreads();
-    {
-      xdft_ip<D, -1>(slot(i0), tw, c, gi, [&](int, int k1, int k2, float2 y) {
-        const int ky = k1 + R1 * k2;
-        if (pk)
-          zA[ky] = y;
-        else
-          Mx[x * PS + ky * NH + kz] = y;
-      });
-      issue(i0 + 2);
-    }
-    float2 dsum[NB2][R2];
-    cp_async_wait<1>();
-    __syncthreads();
-    {
-      xdft_ip<D, -1>(slot(i0 + 1), tw, c, gi, [&](int m2, int k1, int k2, float2 y) {
-        const float w = (float)wavenum(k1 + R1 * k2, NN);
-        dsum[m2][k2] = make_float2(-w * y.y, w * y.x);
-      });
-      issue(i0 + 3);
-    }
-    cp_async_wait<1>();
-    __syncthreads();
-    {
-      xdft_ip<D, -1>(slot(i0 + 2), tw, c, gi, [&](int m2, int k1, int k2, float2 y) {
-        const int ky = k1 + R1 * k2;
-        const float2 d = make_float2(dsum[m2][k2].x + y.x, dsum[m2][k2].y + y.y);
-        if (pk)
-          zB[ky] = d;
-        else
-          Mr[x * PS + ky * NH + kz] = d;
-      });
-      issue(i0 + 4);
-    }
-    if (cb == 0) {  // unpack the kz' = 0 column into kz = 0 and kz = n/2
-      if (c == 0) {
-        for (int ky = gi; ky < NN; ky += GR) {
-          const int km = (NN - ky) & (NN - 1);
-#pragma unroll
-          for (int h = 0; h < 2; h++) {
-            const float2 z = h ? zB[ky] : zA[ky];
-            const float2 zm = h ? zB[km] : zA[km];
-            const float2 s2 = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
-            const float2 d2 = make_float2(0.5f * (z.y + zm.y), -0.5f * (z.x - zm.x));
-            float2* M = h ? Mr : Mx;
-            M[x * PS + ky * NH] = s2;
-            M[x * PS + ky * NH + NQ] = d2;
-          }
-        }
-      }
-    }
-  }
-  cp_async_wait<0>();
-}
-
-template <int NN>
 constexpr int yfwd_tma_smem_bytes() {  // 128 bytes of alignment slack, slots, exchange, tables, barriers
   return 128 + (3 * NN * YDecomp<NN>::T + 2 * NN + 256) * (int)sizeof(float2) + 16;
 }

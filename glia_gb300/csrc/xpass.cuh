@@ -560,144 +560,4 @@ __global__ void __launch_bounds__(256, 2)
   xfwd_finish<EPI>(acc, g, sc, ws, naux == 2);
 }
 
-// xdft with the exchange in the input slot itself: in phase one each thread reads rows
-// R2 a + b of its column and writes rows k1 R2 + b, the same set of rows, so the transposed
-// values can replace the input in place (no exchange buffer); the slot is free after the second
-// barrier.
-template <class D, int S, class Out>
-__device__ __forceinline__ void xdft_ip(float2* sm, const float2* twb, int c, int gi,
-                                        Out&& out) {
-  constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
-  constexpr int NB1 = R2 / GR, NB2 = R1 / GR;
-#pragma unroll
-  for (int m = 0; m < NB1; m++) {
-    const int b = gi + GR * m;
-    float2 u[R1];
-#pragma unroll
-    for (int a = 0; a < R1; a++) u[a] = sm[(R2 * a + b) * T + c];
-    reg_dft<R1, S>(u);
-    const float4* w4 = reinterpret_cast<const float4*>(twb + b * R1);
-#pragma unroll
-    for (int k1 = 0; k1 < R1; k1 += 2) {
-      const float4 w = w4[k1 / 2];
-      if (k1) u[k1] = cmul2(u[k1], make_float2(w.x, w.y));
-      u[k1 + 1] = cmul2(u[k1 + 1], make_float2(w.z, w.w));
-      sm[(k1 * R2 + b) * T + c] = u[k1];
-      sm[((k1 + 1) * R2 + b) * T + c] = u[k1 + 1];
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int m2 = 0; m2 < NB2; m2++) {
-    const int k1 = gi + GR * m2;
-    float2 y[R2];
-#pragma unroll
-    for (int b = 0; b < R2; b++) y[b] = sm[(k1 * R2 + b) * T + c];
-    reg_dft<R2, S>(y);
-#pragma unroll
-    for (int k2 = 0; k2 < R2; k2++) out(m2, k1, k2, y[k2]);
-  }
-  __syncthreads();
-}
-
-template <int NN>
-constexpr int xfwd_ip_smem_bytes() {
-  return (2 * NN * XDecomp<NN>::T + 256) * (int)sizeof(float2);
-}
-
-// k_xfwd_own with each transform exchanging in its own input slot (xdft_ip): 66 KB of shared
-// memory and at most 80 registers per thread, so three CTAs fit on an SM (24 warps instead of
-// 16). The next item enters a slot after the slot's transform has ended (not after its first
-// phase), so each load has a shorter lead; the extra resident CTA covers it.
-template <int NN, int EPI>
-__global__ void __launch_bounds__(256, 3)
-    k_xfwd_ip(Geo g, const float* __restrict__ M2, const float* __restrict__ aux_in,
-              const float* __restrict__ cx, float* __restrict__ out, float* __restrict__ aux_out,
-              float scale, DevScalars* __restrict__ sc, RedWs ws,
-              const float2* __restrict__ tw_g) {
-  using D = XDecomp<NN>;
-  constexpr int R1 = D::R1, R2 = D::R2, T = D::T, GR = 256 / T;
-  constexpr int NB2 = R1 / GR;
-  extern __shared__ float4 xfwd_dyn[];
-  float2* slots = reinterpret_cast<float2*>(xfwd_dyn);  // 2 x NN * T
-  float2* tw = slots + 2 * NN * T;
-  if (EPI == EPI_CGW && sc->status != 0) return;
-  fill_twb<D, -1>(tw, tw_g);
-  const int c = threadIdx.x % T, gi = threadIdx.x / T;
-  const int plane = NN * g.nh, Ns = plane * NN;
-  const int ntiles = plane / T;
-  const float a = EPI == EPI_APPLYD ? 0.f : (float)sc->a_cn;
-  const float pcc = (float)sc->pc_c;
-  const float invN = (float)g.invN;
-  const float2* Mx = reinterpret_cast<const float2*>(M2);
-  const float2* Mr = Mx + Ns;
-  const float2* AX = reinterpret_cast<const float2*>(aux_in);
-  const float2* CX = reinterpret_cast<const float2*>(cx);
-  float2* O = reinterpret_cast<float2*>(out);
-  float2* AO = reinterpret_cast<float2*>(aux_out);
-  const int naux = EPI == EPI_APPLYD ? 0 : (EPI == EPI_SETUP && CX ? 2 : 1);
-  const int NI = 2 + naux;
-  const int mytiles =
-      (int)blockIdx.x < ntiles ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
-                               : 0;
-  const int nitems = NI * mytiles;
-  auto slot = [&](int i) { return slots + (i & 1) * NN * T; };
-  auto issue = [&](int i) {
-    if (i < nitems) {
-      const int t = (int)blockIdx.x + (i / NI) * (int)gridDim.x, kind = i % NI;
-      const float2* src = kind == 0 ? Mx : (kind == 1 ? Mr : (kind == 2 ? AX : CX));
-      stage_tile<NN, T>(slot(i), src, plane, t);
-    }
-    cp_async_commit();
-  };
-  issue(0);
-  issue(1);
-  Acc<float> acc[4];
-  for (int it = 0; it < mytiles; it++) {
-    const int tile = (int)blockIdx.x + it * (int)gridDim.x;
-    const int i0 = NI * it;
-    const XCol col = xcol(g, tile * T + c);
-    float2 dsum[NB2][R2];
-    cp_async_wait<1>();
-    __syncthreads();
-    xdft_ip<D, -1>(slot(i0), tw, c, gi,
-        [&](int m2, int k1, int k2, float2 y) {
-          const float w = (float)wavenum(k1 + R1 * k2, NN);
-          dsum[m2][k2] = make_float2(-w * y.y, w * y.x);
-        });
-    issue(i0 + 2);
-    cp_async_wait<1>();
-    __syncthreads();
-    xdft_ip<D, -1>(slot(i0 + 1), tw, c, gi,
-        [&](int m2, int, int k2, float2 y) {
-          dsum[m2][k2].x += y.x;
-          dsum[m2][k2].y += y.y;
-        });
-    issue(i0 + 3);
-    if (naux == 2) cp_async_wait<0>(); else cp_async_wait<1>();
-    __syncthreads();
-    const float2* SA = slot(i0 + 2);
-    const float2* SX = slot(i0 + 3);
-#pragma unroll
-    for (int m2 = 0; m2 < NB2; m2++) {
-      const int k1 = gi + GR * m2;
-#pragma unroll
-      for (int k2 = 0; k2 < R2; k2++) {
-        const int kx = k1 + R1 * k2;
-        const float2 av = naux ? SA[kx * T + c] : make_float2(0.f, 0.f);
-        const float2 xv = naux == 2 ? SX[kx * T + c] : make_float2(0.f, 0.f);
-        xfwd_epilogue<NN, EPI>(dsum[m2][k2], kx, kx * plane + col.q, col, a, pcc, invN, scale, av,
-                               xv, naux == 2, O, AO, acc);
-      }
-    }
-    if (naux) {
-      __syncthreads();
-      issue(i0 + 4);
-      if (naux == 2) issue(i0 + 5);
-    }
-  }
-  cp_async_wait<0>();
-  xfwd_finish<EPI>(acc, g, sc, ws, naux == 2);
-}
-
 }  // namespace glia
