@@ -27,6 +27,9 @@ those the step would push out of the box) removed. All vectors are FP64 on the h
 objective and gradient is one glia_eval_objective[_and_gradient] call.
 
     python -m glia_gb300.inversion --n 128      # the 128^3 reconstruction, mixed vs FP64
+    python -m glia_gb300.inversion --full256 --precisions mixed,fp64,fp64_plain
+                                                # the 256^3 one; fp64_plain = the
+                                                # reference-structured FP64 engine
 """
 from __future__ import annotations
 
