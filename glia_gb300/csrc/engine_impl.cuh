@@ -471,7 +471,7 @@ class Engine final : public EngineBase {
             g3r_, g3s_, tw256_);
       else if (which == 1 && zpass2_)
         k_zpass2<NN><<<std::min(own_res_[1], pw_blocks_), 256, zpass2_smem_bytes<NN>(),
-                       stream_>>>(g3s_, kxx_, tw256_);
+                       stream_>>>(g3s_, kxx_, tw256_, zrev_);
       else if (which == 1)
         k_zpass<NN><<<std::min(own_res_[1], pw_blocks_), 256, zpass_smem_bytes<NN>(), stream_>>>(
             g3s_, kxx_, tw256_);
@@ -518,6 +518,12 @@ class Engine final : public EngineBase {
         // the even/odd half-length version (k_zpass)
         const char* z2 = std::getenv("GLIA_ZPASS2");
         zpass2_ = !(z2 && z2[0] == '0');
+        // z pass over its line blocks in descending order (default; GLIA_ZREV=0 ascending): the
+        // y-inverse pass before it writes the lines in ascending order, so the z pass starts on
+        // the lines still in L2, and the y-forward pass after it (ascending) starts on the lines
+        // the z pass wrote last
+        const char* zr = std::getenv("GLIA_ZREV");
+        zrev_ = !(zr && zr[0] == '0');
         own_res_[1] = sms_ * (zpass2_ ? per_sm(k_zpass2<NN>, zpass2_smem_bytes<NN>())
                                       : per_sm(k_zpass<NN>, zpass_smem_bytes<NN>()));
         const char* te = std::getenv("GLIA_TMA");
@@ -2434,6 +2440,7 @@ class Engine final : public EngineBase {
   int own_res_[3] = {0, 0, 0};       // ... of the y-inverse pass, the z pass, k_yfwd
   CUtensorMap kmap_{};               // TMA map of the packed line arrays (k_yfwd)
   bool tma_ = false;                 // k_yfwd stages with TMA copies (GLIA_TMA=1)
+  bool zrev_ = true;  // k_zpass2 blocks in descending order
   bool zpass2_ = true;               // z pass with two real lines per complex transform
   bool yinv_bulk_ = true;            // y-inverse rows staged by bulk copies
   bool own_ = false;  // own y and z passes (x pass on): no cuFFT inside the D apply

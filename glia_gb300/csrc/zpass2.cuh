@@ -157,10 +157,13 @@ __device__ __forceinline__ void pair_line(float2* E0, float2* E1, const float4* 
 // block of LB lines: k, H_x, H_y, H_0, through a ring of three shared-memory slots (item i in
 // slot i % 3). k goes to registers first and its slot takes H_0; the H_x / H_y pairs need both
 // slots; then the next block's k and H_x are staged and H_0 is done; then the next H_y is staged.
+// rev: blocks in descending order. The y-inverse pass writes the lines in ascending order and
+// the y-forward pass reads them in ascending order, so in descending order the z pass starts on
+// the lines still in L2 and ends on the ones the y-forward pass reads first.
 template <int NN>
 __global__ void __launch_bounds__(256, 2)
     k_zpass2(float* __restrict__ Hio, const float* __restrict__ kf,
-             const float2* __restrict__ tw_g) {
+             const float2* __restrict__ tw_g, bool rev) {
   using Z = Z2Geom<NN>;
   constexpr int R1 = Z::R1, R2 = Z::R2, KPT = Z::KPT, NQ = Z::NQ, LB = Z::LB, LS = Z::LS;
   constexpr int NP = NN * NN * NQ, PS = Z::PS;
@@ -183,7 +186,8 @@ __global__ void __launch_bounds__(256, 2)
   auto slot = [&](int i) { return slots + (i % 3) * Z::SLOT; };
   auto issue = [&](int i) {
     if (i < nitems) {
-      const int blk = (int)blockIdx.x + (i / 4) * (int)gridDim.x, kind = i % 4;
+      const int bi = (int)blockIdx.x + (i / 4) * (int)gridDim.x, kind = i % 4;
+      const int blk = rev ? Z::NBLK - 1 - bi : bi;
       const char* src =
           kind == 0 ? reinterpret_cast<const char*>(kf + (size_t)blk * LB * NN)
                     : reinterpret_cast<const char*>(Hc + (size_t)(kind - 1) * NP +
@@ -197,7 +201,8 @@ __global__ void __launch_bounds__(256, 2)
   issue(2);
   float kv[2][KPT][R2];  // k of lines l0, l1 at t + R2 ii + R1 k2
   for (int b = 0; b < nblk; b++) {
-    const int i0 = 4 * b, blk = (int)blockIdx.x + b * (int)gridDim.x;
+    const int i0 = 4 * b, bi = (int)blockIdx.x + b * (int)gridDim.x;
+    const int blk = rev ? Z::NBLK - 1 - bi : bi;
     // k -> registers; its slot takes this block's H_0
     cp_async_wait<2>();
     __syncthreads();

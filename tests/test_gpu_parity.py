@@ -348,3 +348,29 @@ def test_gradient_variants_on_own_transforms(variant):
     Jg, grg = g.eval_objective_and_gradient(x, d1)
     assert abs(Jg - Jo) <= 1e-4 * abs(Jo)
     assert rel_l2(grg, gro) < GRAD_TOL
+
+
+@pytest.mark.parametrize("n", [64, 128, 256])
+def test_z_pass_block_order_is_bit_identical(n, monkeypatch):
+    """The z pass over its line blocks in descending order (the default) against ascending order
+    (GLIA_ZREV=0): every line is transformed on its own, so D apply, state and gradient agree
+    bit for bit."""
+    nt = 3
+    wl, tissue, centers = small_problem(n, nt, n_gauss=8)
+    d1 = observation(wl, tissue, centers)
+    f = reference_test_field(n) + 0.1 * tissue.wm.reshape(-1)
+    x = np.concatenate([np.linspace(0.1, 0.9, len(centers)), [wl.kappa, wl.rho]])
+    out = []
+    for on in ("1", "0"):
+        monkeypatch.setenv("GLIA_ZREV", on)
+        g = gpu(n, MIXED)
+        configure(g, wl, tissue, centers)
+        g.set_obs_filter(np.ones(n ** 3))
+        c0 = g.phi_apply(np.linspace(0.2, 1.0, len(centers)))
+        J, gr = g.eval_objective_and_gradient(x, d1)
+        out.append((g.apply_d(f), g.solve_state(c0), J, gr))
+        g.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
+    assert np.array_equal(out[0][3], out[1][3])
