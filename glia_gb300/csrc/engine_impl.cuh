@@ -2440,7 +2440,7 @@ class Engine final : public EngineBase {
   int own_res_[3] = {0, 0, 0};       // ... of the y-inverse pass, the z pass, k_yfwd
   CUtensorMap kmap_{};               // TMA map of the packed line arrays (k_yfwd)
   bool tma_ = false;                 // k_yfwd stages with TMA copies (GLIA_TMA=1)
-  bool zrev_ = true;  // k_zpass2 blocks in descending order
+  bool zrev_ = true;                 // k_zpass2 line blocks in descending order
   bool zpass2_ = true;               // z pass with two real lines per complex transform
   bool yinv_bulk_ = true;            // y-inverse rows staged by bulk copies
   bool own_ = false;  // own y and z passes (x pass on): no cuFFT inside the D apply
